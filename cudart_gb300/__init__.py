@@ -1,0 +1,12 @@
+"""GB300-native (sm_103a) Monte Carlo path-tracing hot path of CudaRT.
+
+The compute path is the in-tree shared library libcrt_gb300.so (C ABI in
+include/crt_gb300.h); this package is its host-side mirror of the
+reference's renderer interface plus the seeded synthetic workloads.
+"""
+from ._lib import CrtError, load
+from .renderer import GB300Renderer, GB300Scene, bvh_build_host, camera_from_json
+from . import scenes
+
+__all__ = ["CrtError", "GB300Renderer", "GB300Scene", "bvh_build_host", "camera_from_json",
+           "load", "scenes"]

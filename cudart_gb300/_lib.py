@@ -1,0 +1,115 @@
+"""ctypes binding of libcrt_gb300.so (the C ABI declared in include/crt_gb300.h).
+
+The library is built in-tree (cudart_gb300/libcrt_gb300.so).  There is no
+fallback: if the shared library is missing or fails to load, every entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcrt_gb300.so")
+
+CRT_OK = 0
+STATUS_NAMES = {0: "CRT_OK", 1: "CRT_ERR_INVALID", 2: "CRT_ERR_CUDA", 3: "CRT_ERR_NOMEM",
+                4: "CRT_ERR_UNSUPPORTED", 5: "CRT_ERR_WATCHDOG", 6: "CRT_ERR_LIMIT"}
+
+MODE_MEGAKERNEL = 0
+MODE_WAVEFRONT = 1
+
+
+class CrtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Material(C.Structure):
+    _fields_ = [("bsdf", C.c_int32), ("texture", C.c_int32), ("kd", C.c_float * 3),
+                ("ka", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
+                ("ni", C.c_float), ("diffuse", C.c_float)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("dir", C.c_float * 3), ("up", C.c_float * 3),
+                ("right", C.c_float * 3), ("fov", C.c_float), ("aspect", C.c_float),
+                ("aperture", C.c_float), ("focus", C.c_float), ("xpixels", C.c_int32),
+                ("ypixels", C.c_int32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("positions", C.c_void_p),
+                ("normals", C.c_void_p), ("uvs", C.c_void_p), ("material_ids", C.c_void_p),
+                ("num_materials", C.c_uint32), ("materials", C.c_void_p),
+                ("num_lights", C.c_uint32), ("light_indices", C.c_void_p),
+                ("num_textures", C.c_uint32), ("texture_dims", C.c_void_p),
+                ("texels", C.c_void_p)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("num_nodes", C.c_uint32),
+                ("max_depth", C.c_uint32), ("num_lights", C.c_uint32),
+                ("num_materials", C.c_uint32), ("num_textures", C.c_uint32),
+                ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64),
+                ("shading_bytes", C.c_uint64), ("texture_bytes", C.c_uint64),
+                ("lights_area", C.c_float), ("build_ms", C.c_float)]
+
+
+class RenderOptions(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("seed", C.c_uint64), ("view_id", C.c_uint32),
+                ("mode", C.c_uint32), ("block_size", C.c_uint32), ("wave_paths", C.c_uint32)]
+
+
+# name -> (restype, argtypes); every entry point of include/crt_gb300.h
+P, U32, U64, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float
+SIGNATURES = {
+    "crt_api_version": (C.c_int, []),
+    "crt_last_error": (C.c_char_p, []),
+    "crt_camera_from_json": (C.c_int, [F, F, F, P, P, P, U32, U32, P]),
+    "crt_scene_create": (C.c_int, [P, P]),
+    "crt_scene_destroy": (C.c_int, [P]),
+    "crt_scene_get_info": (C.c_int, [P, P]),
+    "crt_scene_export_bvh": (C.c_int, [P, P, P]),
+    "crt_bvh_build_host": (C.c_int, [P, U32, P, P, P, P]),
+    "crt_trace_closest": (C.c_int, [P, P, U32, P, P, P, P]),
+    "crt_trace_counts": (C.c_int, [P, P, U32, P, P, P]),
+    "crt_render_options_default": (None, [P]),
+    "crt_render_create": (C.c_int, [P, P, U32, U32, P, P]),
+    "crt_render_destroy": (C.c_int, [P]),
+    "crt_render_pass": (C.c_int, [P, U32]),
+    "crt_render_samples_rendered": (C.c_int, [P, P]),
+    "crt_render_synchronize": (C.c_int, [P]),
+    "crt_render_resolve": (C.c_int, [P, P]),
+    "crt_render_accum": (C.c_int, [P, P]),
+    "crt_render_accum_device": (C.c_int, [P, P]),
+    "crt_render_reset": (C.c_int, [P]),
+    "crt_render_set_camera": (C.c_int, [P, P]),
+    "crt_render_set_stream": (C.c_int, [P, P]),
+    "crt_render_ray_counts": (C.c_int, [P, P, P]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load libcrt_gb300.so, building nothing: a missing library is an error."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing; run `python -m cudart_gb300.build` "
+                              "(or __graft_entry__.build()) first")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != CRT_OK:
+        msg = load().crt_last_error()
+        raise CrtError(status, msg.decode() if msg else "")

@@ -1,0 +1,60 @@
+// bvh8.h -- host build of the 8-wide BVH with quantised child bounds.
+//
+// Replaces the reference's binary SAH build (src/geometry/bvh.cpp:65-323,
+// 32-byte LinearBVHNode, two 1-D textures on the GPU) with:
+//   1. a binned surface-area-heuristic binary build (leaves of <= 3
+//      triangles, the reference's maxTrisInNode, bvh.cpp:62);
+//   2. a greedy collapse to 8-wide nodes (open the child with the largest
+//      surface area until 8 children);
+//   3. child slots ordered by octant so that visiting slot k ^ octant(ray)
+//      is approximately front to back;
+//   4. child boxes quantised to 8 bits per plane relative to the node
+//      origin with a power-of-two scale, rounded outward (conservative).
+// Every triangle box is widened by a margin proportional to the scene's
+// coordinate magnitude before the build, so the GPU's rounded slab tests
+// never cull a triangle that the exact Moller-Trumbore test accepts.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace crt {
+
+// 80-byte node, read on the GPU as five 16-byte loads.
+struct alignas(16) Bvh8Node {
+    float px, py, pz;          // quantisation origin
+    uint8_t ex, ey, ez;        // biased exponents of the per-axis scale 2^(e-127)
+    uint8_t imask;             // bit s: slot s is an internal node
+    uint32_t child_base;       // index of the first internal child
+    uint32_t tri_base;         // index of the first triangle record of the leaves
+    uint8_t meta[8];           // 0 empty, 0x80 internal, else (count << 5) | offset
+    uint8_t qlo[3][8];         // [axis][slot]
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(Bvh8Node) == 80, "node layout");
+
+// 48-byte intersection record: v1.xyz + face index (bits), e1.xyz, e2.xyz.
+struct alignas(16) TriRecord {
+    float v1[3];
+    uint32_t face;
+    float e1[3];
+    float pad1;
+    float e2[3];
+    float pad2;
+};
+static_assert(sizeof(TriRecord) == 48, "triangle layout");
+
+struct Bvh8 {
+    std::vector<Bvh8Node> nodes;
+    std::vector<TriRecord> tris;     // in leaf order
+    uint32_t max_depth = 0;
+    float margin = 0.f;
+};
+
+// v1/e1/e2: [n][3] floats as the scene computes them (e = v - v1, in FP32).
+// Returns false (with msg) if the scene is empty or the tree exceeds
+// max_levels levels.
+bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
+                uint32_t max_levels, Bvh8& out, const char** msg);
+
+}  // namespace crt

@@ -1,0 +1,283 @@
+// render.cu -- progressive rendering: the plain megakernel (drop-in for the
+// reference's renderKernel, src/renderer/parallel_renderer.cu:318-342), the
+// output resolve, and the crt_render_* C ABI.  The wavefront form lives in
+// wavefront.cu and shares the path state machine below.
+#include "crt_internal.h"
+#include "render_common.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace crt {
+
+int grid_for(uint32_t n, int block, int per_sm);
+int wavefront_pass(crt_render r, uint32_t spp0, uint32_t nspp);
+
+constexpr int kMegaBlock = 128;         // 16 x 8 pixel tile, warps of 8 x 4
+constexpr uint32_t kMegaSppPerLaunch = 4;
+
+// One thread per pixel; samples [spp0, spp0 + nspp) are added to the FP32
+// accumulator in sample order, so the sums equal the reference's per-pass
+// accumulation (`p_imgBuffer[idx] += color`, parallel_renderer.cu:340).
+__global__ void __launch_bounds__(kMegaBlock) mega_kernel(RenderParams P) {
+    __shared__ uint2 stack_sh[kStackShared * kMegaBlock];
+    Stack st;
+    st.sh = stack_sh + threadIdx.x;
+    st.stride = kMegaBlock;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t x = blockIdx.x * 16u + (warp & 1u) * 8u + (lane & 7u);
+    const uint32_t y = blockIdx.y * 8u + (warp >> 1) * 4u + (lane >> 3);
+    uint32_t n_ext = 0, n_shadow = 0;
+    if (x < P.width && y < P.height) {
+        const uint32_t pixel = y * P.width + x;
+        float4 acc = P.accum[pixel];
+        for (uint32_t s = 0; s < P.nspp; ++s) {
+            const float3 c = sample_path(P, (int)x, (int)y, pixel, P.spp0 + s, st, n_ext, n_shadow);
+            acc.x = acc.x + c.x;
+            acc.y = acc.y + c.y;
+            acc.z = acc.z + c.z;
+        }
+        P.accum[pixel] = acc;
+    }
+    count_rays(P.ray_counts, n_ext, n_shadow);
+}
+
+// float3ToUchar4 (renderer.h:149-156) of sum / spp, then the host-side
+// gammaCorrectPixel (renderer.cu:495-504) as a 256-entry table.
+__global__ void resolve_kernel(const float4* __restrict__ accum, uint32_t n, float spp,
+                               const uint8_t* __restrict__ lut, uchar4* __restrict__ out) {
+    __shared__ uint8_t L[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) L[i] = lut[i];
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = accum[i];
+        const float vx = a.x / spp, vy = a.y / spp, vz = a.z / spp;
+        const uint32_t qx = (uint32_t)((vx > 1.0f ? 1.0f : vx) * 255.f);
+        const uint32_t qy = (uint32_t)((vy > 1.0f ? 1.0f : vy) * 255.f);
+        const uint32_t qz = (uint32_t)((vz > 1.0f ? 1.0f : vz) * 255.f);
+        out[i] = make_uchar4(L[qx & 255u], L[qy & 255u], L[qz & 255u], 255u);
+    }
+}
+
+__global__ void unpack_accum_kernel(const float4* __restrict__ accum, uint32_t n, float* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = accum[i];
+        out[3ull * i] = a.x;
+        out[3ull * i + 1] = a.y;
+        out[3ull * i + 2] = a.z;
+    }
+}
+
+Camera to_device_camera(const crt_camera& c) {
+    Camera d;
+    d.eye = make_float3(c.eye[0], c.eye[1], c.eye[2]);
+    d.dir = make_float3(c.dir[0], c.dir[1], c.dir[2]);
+    d.up = make_float3(c.up[0], c.up[1], c.up[2]);
+    d.right = make_float3(c.right[0], c.right[1], c.right[2]);
+    d.fov = c.fov;
+    d.aspect = c.aspect;
+    d.aperture = c.aperture;
+    d.focus = c.focus;
+    d.xpixels = c.xpixels;
+    d.ypixels = c.ypixels;
+    return d;
+}
+
+RenderParams make_params(crt_render r, uint32_t spp0, uint32_t nspp) {
+    RenderParams P;
+    P.S = r->scene->dev;
+    P.cam = r->cam;
+    P.accum = r->accum.as<float4>();
+    P.width = r->width;
+    P.height = r->height;
+    P.seed = r->opts.seed;
+    P.view = r->opts.view_id;
+    P.spp0 = spp0;
+    P.nspp = nspp;
+    P.max_depth = r->opts.max_depth;
+    P.ray_counts = r->ray_counts.as<unsigned long long>();
+    return P;
+}
+
+int check_device_error(crt_render r) {
+    uint32_t err = 0;
+    CRT_CUDA(cudaMemcpyAsync(&err, r->scene->error.p, 4, cudaMemcpyDeviceToHost, r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    if (err & ERR_WATCHDOG) return set_error(CRT_ERR_WATCHDOG, "traversal exceeded its node-visit limit");
+    if (err & ERR_STACK) return set_error(CRT_ERR_WATCHDOG, "traversal stack overflow");
+    return CRT_OK;
+}
+
+}  // namespace crt
+
+using namespace crt;
+
+extern "C" {
+
+void crt_render_options_default(crt_render_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->max_depth = 6;           // c_maxBounces (renderer.cu:25,33)
+    o->seed = 1234;             // the reference's curand seed (parallel_renderer.cu:315)
+    o->view_id = 0;
+    o->mode = CRT_MODE_MEGAKERNEL;
+    o->block_size = 0;
+    o->wave_paths = 0;
+}
+
+int crt_render_create(crt_scene s, const crt_camera* cam, uint32_t width, uint32_t height,
+                      const crt_render_options* opts, crt_render* out) {
+    if (!s || !cam || !out) return set_error(CRT_ERR_INVALID, "crt_render_create: null argument");
+    if (width == 0 || height == 0 || (uint64_t)width * height >= (1ull << 31))
+        return set_error(CRT_ERR_INVALID, "crt_render_create: bad image size");
+    *out = nullptr;
+    crt_render r = new crt_render_s();
+    r->scene = s;
+    r->width = width;
+    r->height = height;
+    if (opts) r->opts = *opts;
+    else crt_render_options_default(&r->opts);
+    if (r->opts.max_depth == 0 || r->opts.max_depth > 1024) {
+        delete r;
+        return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
+    }
+    if (r->opts.mode > CRT_MODE_WAVEFRONT) { delete r; return set_error(CRT_ERR_INVALID, "unknown mode"); }
+    r->cam = to_device_camera(*cam);
+    const uint64_t npix = (uint64_t)width * height;
+    cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) r->own_stream = true;
+    if (e == cudaSuccess) e = r->accum.alloc(npix * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->accum.p, 0, npix * sizeof(float4), r->stream);
+    if (e == cudaSuccess) e = r->ray_counts.alloc(2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->ray_counts.p, 0, 2 * sizeof(unsigned long long), r->stream);
+    // gammaCorrectPixel (renderer.cu:495-504) runs on the host in the
+    // reference; the same powf per byte value gives the table.
+    uint8_t lut[256];
+    const float inv_gamma = 1.f / 2.2f;
+    for (int v = 0; v < 256; ++v) lut[v] = (uint8_t)(powf((float)v * 1.f / 255.f, inv_gamma) * 255.f);
+    if (e == cudaSuccess) e = r->lut.alloc(256);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->lut.p, lut, 256, cudaMemcpyHostToDevice, r->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+    if (e != cudaSuccess) {
+        int st = cuda_error(e, "crt_render_create");
+        if (r->own_stream) cudaStreamDestroy(r->stream);
+        delete r;
+        return st;
+    }
+    *out = r;
+    return CRT_OK;
+}
+
+int crt_render_destroy(crt_render r) {
+    if (!r) return CRT_OK;
+    if (r->stream) cudaStreamSynchronize(r->stream);
+    if (r->own_stream) cudaStreamDestroy(r->stream);
+    delete r;
+    return CRT_OK;
+}
+
+int crt_render_set_stream(crt_render r, void* stream) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    if (r->own_stream) cudaStreamDestroy(r->stream);
+    r->stream = (cudaStream_t)stream;
+    r->own_stream = false;
+    destroy_wave_graph(r->wave_graph);
+    r->wave_graph = nullptr;
+    return CRT_OK;
+}
+
+int crt_render_set_camera(crt_render r, const crt_camera* cam) {
+    if (!r || !cam) return set_error(CRT_ERR_INVALID, "null argument");
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    r->cam = to_device_camera(*cam);
+    destroy_wave_graph(r->wave_graph);   // the captured launches hold the old camera
+    r->wave_graph = nullptr;
+    return CRT_OK;
+}
+
+int crt_render_pass(crt_render r, uint32_t n_spp) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    if (n_spp == 0) return CRT_OK;
+    if ((uint64_t)r->samples_rendered + n_spp >= (1ull << 32))
+        return set_error(CRT_ERR_LIMIT, "sample counter overflow");
+    if (r->opts.mode == CRT_MODE_WAVEFRONT) {
+        int st = wavefront_pass(r, r->samples_rendered, n_spp);
+        if (st != CRT_OK) return st;
+    } else {
+        dim3 grid((r->width + 15) / 16, (r->height + 7) / 8);
+        for (uint32_t done = 0; done < n_spp;) {
+            uint32_t k = n_spp - done < kMegaSppPerLaunch ? n_spp - done : kMegaSppPerLaunch;
+            mega_kernel<<<grid, kMegaBlock, 0, r->stream>>>(make_params(r, r->samples_rendered + done, k));
+            done += k;
+        }
+        CRT_CUDA(cudaGetLastError());
+    }
+    r->samples_rendered += n_spp;
+    return CRT_OK;
+}
+
+int crt_render_samples_rendered(crt_render r, uint32_t* out) {
+    if (!r || !out) return set_error(CRT_ERR_INVALID, "null argument");
+    *out = r->samples_rendered;
+    return CRT_OK;
+}
+
+int crt_render_synchronize(crt_render r) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    return check_device_error(r);
+}
+
+int crt_render_resolve(crt_render r, uint8_t* host_rgba) {
+    if (!r || !host_rgba) return set_error(CRT_ERR_INVALID, "null argument");
+    if (r->samples_rendered == 0) return set_error(CRT_ERR_INVALID, "no samples rendered");
+    const uint32_t n = r->width * r->height;
+    DevBuf out;
+    CRT_CUDA(out.alloc((size_t)n * 4));
+    resolve_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>(), n,
+                                                              (float)r->samples_rendered,
+                                                              r->lut.as<uint8_t>(), out.as<uchar4>());
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaMemcpyAsync(host_rgba, out.p, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    return check_device_error(r);
+}
+
+int crt_render_accum(crt_render r, float* host_rgb) {
+    if (!r || !host_rgb) return set_error(CRT_ERR_INVALID, "null argument");
+    const uint32_t n = r->width * r->height;
+    DevBuf out;
+    CRT_CUDA(out.alloc((size_t)n * 12));
+    unpack_accum_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>(), n, out.as<float>());
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaMemcpyAsync(host_rgb, out.p, (size_t)n * 12, cudaMemcpyDeviceToHost, r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    return check_device_error(r);
+}
+
+int crt_render_accum_device(crt_render r, float** d_rgb) {
+    if (!r || !d_rgb) return set_error(CRT_ERR_INVALID, "null argument");
+    *d_rgb = r->accum.as<float>();   // [n][4]: rgb + unused
+    return CRT_OK;
+}
+
+int crt_render_reset(crt_render r) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    CRT_CUDA(cudaMemsetAsync(r->accum.p, 0, r->accum.bytes, r->stream));
+    CRT_CUDA(cudaMemsetAsync(r->ray_counts.p, 0, r->ray_counts.bytes, r->stream));
+    r->samples_rendered = 0;
+    return CRT_OK;
+}
+
+int crt_render_ray_counts(crt_render r, uint64_t* ext, uint64_t* shadow) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    unsigned long long c[2] = {0, 0};
+    CRT_CUDA(cudaMemcpyAsync(c, r->ray_counts.p, sizeof(c), cudaMemcpyDeviceToHost, r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    if (ext) *ext = c[0];
+    if (shadow) *shadow = c[1];
+    return CRT_OK;
+}
+
+}  // extern "C"

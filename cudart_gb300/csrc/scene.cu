@@ -1,0 +1,290 @@
+// scene.cu -- scene construction, upload and the library's error handling.
+//
+// Replaces the reference's scene preparation (src/geometry/scene.cpp:74-165)
+// and the ParallelRenderer uploads (src/renderer/parallel_renderer.cu:37-279):
+// triangles become 48-byte intersection records in BVH leaf order plus
+// per-face shading records, materials a small float4 table, and the BVH an
+// 8-wide quantised tree (bvh8.cpp) instead of two 1-D textures.
+#include "crt_internal.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+namespace crt {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int status, const std::string& msg) {
+    g_last_error = msg;
+    return status;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+    return set_error(CRT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+template <typename T>
+int upload(DevBuf& b, const std::vector<T>& v) {
+    size_t bytes = v.size() * sizeof(T);
+    cudaError_t e = b.alloc(bytes ? bytes : 16);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMalloc");
+    if (bytes) {
+        e = cudaMemcpy(b.p, v.data(), bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_error(e, "cudaMemcpy");
+    }
+    return CRT_OK;
+}
+
+inline float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+inline float bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline float bits(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
+
+}  // namespace
+}  // namespace crt
+
+using namespace crt;
+
+extern "C" {
+
+int crt_api_version(void) { return CRT_API_VERSION; }
+
+const char* crt_last_error(void) { return g_last_error.c_str(); }
+
+int crt_camera_from_json(float fov_deg, float focal_length, float fstop, const float eye[3],
+                         const float view_dir[3], const float up[3], uint32_t width,
+                         uint32_t height, crt_camera* out) {
+    // CameraJsonLoader::getCamera (src/context/json_loader.cpp:26-48), in FP32
+    // with the same double-precision degree conversion.
+    if (!eye || !view_dir || !up || !out || width == 0 || height == 0)
+        return set_error(CRT_ERR_INVALID, "crt_camera_from_json: bad argument");
+    auto norm = [](const float* v, float* o) {
+        float n = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        o[0] = v[0] / n; o[1] = v[1] / n; o[2] = v[2] / n;
+    };
+    out->xpixels = (int32_t)width;
+    out->ypixels = (int32_t)height;
+    out->fov = tanf((float)((double)(fov_deg * 0.5f) * 3.14159265358979323846 / 180.0));
+    for (int k = 0; k < 3; ++k) out->eye[k] = eye[k];
+    out->focus = sqrtf(view_dir[0] * view_dir[0] + view_dir[1] * view_dir[1] + view_dir[2] * view_dir[2]);
+    norm(view_dir, out->dir);
+    norm(up, out->up);
+    float r[3] = {out->dir[1] * out->up[2] - out->dir[2] * out->up[1],
+                  out->dir[2] * out->up[0] - out->dir[0] * out->up[2],
+                  out->dir[0] * out->up[1] - out->dir[1] * out->up[0]};
+    norm(r, out->right);
+    out->aperture = focal_length / fstop;
+    out->aspect = (float)width / (float)height;
+    return CRT_OK;
+}
+
+int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
+    if (!d || !out) return set_error(CRT_ERR_INVALID, "crt_scene_create: null argument");
+    *out = nullptr;
+    const uint32_t n = d->num_triangles;
+    if (n == 0 || !d->positions || !d->normals || !d->material_ids)
+        return set_error(CRT_ERR_INVALID, "scene needs triangles, normals and material ids");
+    if (d->num_materials == 0 || !d->materials)
+        return set_error(CRT_ERR_INVALID, "scene has no materials");
+    if (n >= (1u << 31)) return set_error(CRT_ERR_LIMIT, "more than 2^31 triangles");
+    for (uint32_t i = 0; i < n; ++i)
+        if (d->material_ids[i] >= d->num_materials)
+            return set_error(CRT_ERR_INVALID, "material id out of range at face " + std::to_string(i));
+    for (uint32_t m = 0; m < d->num_materials; ++m) {
+        int t = d->materials[m].texture;
+        if (t != CRT_NO_TEXTURE && (t < 0 || (uint32_t)t >= d->num_textures))
+            return set_error(CRT_ERR_INVALID, "texture index out of range in material " + std::to_string(m));
+        if (d->materials[m].bsdf < 0 || d->materials[m].bsdf > CRT_BSDF_EMISSIVE)
+            return set_error(CRT_ERR_INVALID, "unknown bsdf in material " + std::to_string(m));
+    }
+    if (d->num_textures && (!d->texture_dims || !d->texels))
+        return set_error(CRT_ERR_INVALID, "textures need dims and texels");
+
+    auto t0 = std::chrono::steady_clock::now();
+    crt_scene s = new crt_scene_s();
+
+    // Triangle geometry as Scene::loadTriangles computes it (scene.cpp:111-130).
+    std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n), area(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* p = d->positions + 9ull * i;
+        for (int k = 0; k < 3; ++k) {
+            v1[3 * i + k] = p[k];
+            e1[3 * i + k] = p[3 + k] - p[k];
+            e2[3 * i + k] = p[6 + k] - p[k];
+        }
+        const float* a = &e1[3 * i];
+        const float* b = &e2[3 * i];
+        float cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+        area[i] = sqrtf(cx * cx + cy * cy + cz * cz) / 2.0f;
+    }
+    // Light list (scene.cpp:148-160) and total light area (scene.cpp:167-173).
+    if (d->num_lights) {
+        if (!d->light_indices) { delete s; return set_error(CRT_ERR_INVALID, "light_indices is null"); }
+        for (uint32_t i = 0; i < d->num_lights; ++i) {
+            if (d->light_indices[i] >= n) { delete s; return set_error(CRT_ERR_INVALID, "light index out of range"); }
+            s->lights.push_back(d->light_indices[i]);
+        }
+    } else {
+        for (uint32_t i = 0; i < n; ++i)
+            if (d->materials[d->material_ids[i]].bsdf == CRT_BSDF_EMISSIVE) s->lights.push_back(i);
+    }
+    if (s->lights.empty()) {
+        delete s;
+        return set_error(CRT_ERR_INVALID, "scene has no emissive triangles (light sampling needs one)");
+    }
+    float lights_area = 0;
+    for (uint32_t f : s->lights) lights_area += area[f];
+    // Host-side validation is complete; from here on a device is needed.
+    cudaError_t dev_err = cudaGetDevice(&s->device);
+    if (dev_err != cudaSuccess) { delete s; return cuda_error(dev_err, "cudaGetDevice"); }
+
+    const char* msg = nullptr;
+    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, s->bvh, &msg)) {
+        delete s;
+        return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
+    }
+
+    // Per-face shading records.
+    std::vector<float4> shade(3ull * n), uvs(2ull * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* nn = d->normals + 9ull * i;
+        shade[3 * i + 0] = f4(nn[0], nn[1], nn[2], nn[3]);
+        shade[3 * i + 1] = f4(nn[4], nn[5], nn[6], nn[7]);
+        shade[3 * i + 2] = f4(nn[8], area[i], bits(d->material_ids[i]), 0.f);
+        if (d->uvs) {
+            const float* t = d->uvs + 6ull * i;
+            uvs[2 * i + 0] = f4(t[0], t[1], t[2], t[3]);
+            uvs[2 * i + 1] = f4(t[4], t[5], 0.f, 0.f);
+        } else {
+            uvs[2 * i + 0] = uvs[2 * i + 1] = f4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    // Materials (createMaterialsData, parallel_renderer.cu:252-279) with the
+    // emission scaling ka = Ka * 3 * lightsArea (scene.cpp:163,177).
+    std::vector<float4> mats(4ull * d->num_materials);
+    for (uint32_t m = 0; m < d->num_materials; ++m) {
+        const crt_material& M = d->materials[m];
+        float ka[3];
+        for (int k = 0; k < 3; ++k) ka[k] = (M.ka[k] * 3.0f) * lights_area;
+        mats[4 * m + 0] = f4(M.kd[0], M.kd[1], M.kd[2], bits((int32_t)M.texture));
+        mats[4 * m + 1] = f4(ka[0], ka[1], ka[2], bits((int32_t)M.bsdf));
+        mats[4 * m + 2] = f4(M.ks[0], M.ks[1], M.ks[2], M.ns);
+        mats[4 * m + 3] = f4(M.ni, M.diffuse, 0.f, 0.f);
+    }
+    std::vector<float4> lgeo(3 * s->lights.size());
+    for (size_t i = 0; i < s->lights.size(); ++i) {
+        uint32_t f = s->lights[i];
+        lgeo[3 * i + 0] = f4(v1[3 * f], v1[3 * f + 1], v1[3 * f + 2], bits(f));
+        lgeo[3 * i + 1] = f4(e1[3 * f], e1[3 * f + 1], e1[3 * f + 2], area[f]);
+        lgeo[3 * i + 2] = f4(e2[3 * f], e2[3 * f + 1], e2[3 * f + 2], bits(d->material_ids[f]));
+    }
+    // Textures flattened in order, then as many zero texels as the last
+    // texture is wide (texture_store.cpp:68-70).
+    std::vector<float4> texels;
+    std::vector<uint2> dims;
+    std::vector<uint32_t> offs;
+    uint64_t total = 0;
+    for (uint32_t t = 0; t < d->num_textures; ++t) {
+        uint32_t w = d->texture_dims[2 * t], h = d->texture_dims[2 * t + 1];
+        if (w == 0 || h == 0) { delete s; return set_error(CRT_ERR_INVALID, "empty texture"); }
+        dims.push_back(make_uint2(w, h));
+        offs.push_back((uint32_t)total);
+        total += (uint64_t)w * h;
+        if (total >= (1ull << 31)) { delete s; return set_error(CRT_ERR_LIMIT, "texture data too large"); }
+    }
+    texels.reserve(total + (d->num_textures ? dims.back().x : 0));
+    for (uint64_t i = 0; i < total; ++i)
+        texels.push_back(f4(d->texels[3 * i], d->texels[3 * i + 1], d->texels[3 * i + 2], 0.f));
+    if (d->num_textures)
+        for (uint32_t i = 0; i < dims.back().x; ++i) texels.push_back(f4(0.f, 0.f, 0.f, 0.f));
+
+    int st = CRT_OK;
+    if ((st = upload(s->nodes, s->bvh.nodes)) || (st = upload(s->tris, s->bvh.tris)) ||
+        (st = upload(s->shade, shade)) || (st = upload(s->uvs, uvs)) || (st = upload(s->mats, mats)) ||
+        (st = upload(s->light_geo, lgeo)) || (st = upload(s->texels, texels)) ||
+        (st = upload(s->tex_dims, dims)) || (st = upload(s->tex_offsets, offs))) {
+        delete s;
+        return st;
+    }
+    cudaError_t e = s->error.alloc(16);
+    if (e == cudaSuccess) e = cudaMemset(s->error.p, 0, 16);
+    if (e != cudaSuccess) { delete s; return cuda_error(e, "error word"); }
+
+    DevScene& D = s->dev;
+    D.nodes = s->nodes.as<float4>();
+    D.tris = s->tris.as<float4>();
+    D.shade = s->shade.as<float4>();
+    D.uvs = s->uvs.as<float4>();
+    D.mats = s->mats.as<float4>();
+    D.light_geo = s->light_geo.as<float4>();
+    D.texels = s->texels.as<float4>();
+    D.tex_dims = s->tex_dims.as<uint2>();
+    D.tex_offsets = s->tex_offsets.as<uint32_t>();
+    D.tex_total = (uint32_t)texels.size();
+    D.n_lights = (uint32_t)s->lights.size();
+    D.lights_area = lights_area;
+    D.n_faces = n;
+    D.error = s->error.as<uint32_t>();
+
+    crt_scene_info& I = s->info;
+    I.num_triangles = n;
+    I.num_nodes = (uint32_t)s->bvh.nodes.size();
+    I.max_depth = s->bvh.max_depth;
+    I.num_lights = D.n_lights;
+    I.num_materials = d->num_materials;
+    I.num_textures = d->num_textures;
+    I.node_bytes = s->bvh.nodes.size() * sizeof(Bvh8Node);
+    I.triangle_bytes = s->bvh.tris.size() * sizeof(TriRecord);
+    I.shading_bytes = (shade.size() + uvs.size()) * sizeof(float4);
+    I.texture_bytes = texels.size() * sizeof(float4);
+    I.lights_area = lights_area;
+    I.build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    *out = s;
+    return CRT_OK;
+}
+
+int crt_scene_destroy(crt_scene s) {
+    delete s;
+    return CRT_OK;
+}
+
+int crt_scene_get_info(crt_scene s, crt_scene_info* out) {
+    if (!s || !out) return set_error(CRT_ERR_INVALID, "crt_scene_get_info: null argument");
+    *out = s->info;
+    return CRT_OK;
+}
+
+int crt_scene_export_bvh(crt_scene s, void* nodes, void* triangles) {
+    if (!s) return set_error(CRT_ERR_INVALID, "crt_scene_export_bvh: null scene");
+    if (nodes) std::memcpy(nodes, s->bvh.nodes.data(), s->bvh.nodes.size() * sizeof(Bvh8Node));
+    if (triangles) std::memcpy(triangles, s->bvh.tris.data(), s->bvh.tris.size() * sizeof(TriRecord));
+    return CRT_OK;
+}
+
+int crt_bvh_build_host(const float* positions, uint32_t n, uint32_t* num_nodes,
+                       uint32_t* max_depth, void* nodes, void* triangles) {
+    if (!positions || n == 0) return set_error(CRT_ERR_INVALID, "crt_bvh_build_host: no triangles");
+    std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n);
+    for (uint32_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const float* p = positions + 9ull * i;
+            v1[3 * i + k] = p[k];
+            e1[3 * i + k] = p[3 + k] - p[k];
+            e2[3 * i + k] = p[6 + k] - p[k];
+        }
+    Bvh8 b;
+    const char* msg = nullptr;
+    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, b, &msg))
+        return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
+    if (num_nodes) *num_nodes = (uint32_t)b.nodes.size();
+    if (max_depth) *max_depth = b.max_depth;
+    if (nodes) std::memcpy(nodes, b.nodes.data(), b.nodes.size() * sizeof(Bvh8Node));
+    if (triangles) std::memcpy(triangles, b.tris.data(), b.tris.size() * sizeof(TriRecord));
+    return CRT_OK;
+}
+
+}  // extern "C"

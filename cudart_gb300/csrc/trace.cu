@@ -1,0 +1,86 @@
+// trace.cu -- batched closest-hit queries (crt_trace_closest) and the
+// instrumented traversal that counts node visits and triangle tests per ray.
+//
+// Replaces intersectBVH (src/renderer/renderer.cu:283-330) for batches of
+// arbitrary rays.  One thread per ray, 128-thread blocks, grid-stride loop
+// over a grid that is a multiple of the SM count.
+#include "crt_internal.h"
+
+namespace crt {
+
+constexpr int kTraceBlock = 128;
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceBlock) trace_closest_kernel(DevScene S, const float4* __restrict__ rays,
+                                                                    uint32_t n, int32_t* __restrict__ out_face,
+                                                                    float* __restrict__ out_t,
+                                                                    float2* __restrict__ out_uv,
+                                                                    uint32_t* __restrict__ out_nodes,
+                                                                    uint32_t* __restrict__ out_tris) {
+    __shared__ uint2 stack_sh[kStackShared * kTraceBlock];
+    Stack st;
+    st.sh = stack_sh + threadIdx.x;
+    st.stride = kTraceBlock;
+    for (uint32_t i = blockIdx.x * kTraceBlock + threadIdx.x; i < n; i += gridDim.x * kTraceBlock) {
+        const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
+        Hit h;
+        h.t = b.w;
+        h.face = -1;
+        h.u = h.v = 0.f;
+        TraversalStats ts{0, 0};
+        traverse<false, COUNT>(S, xyz(a), xyz(b), a.w, h, -1, st, &ts);
+        if (COUNT) {
+            out_nodes[i] = ts.nodes;
+            out_tris[i] = ts.tris;
+        } else {
+            out_face[i] = h.face;
+            out_t[i] = h.face >= 0 ? h.t : FLT_MAX;
+            if (out_uv) out_uv[i] = make_float2(h.u, h.v);
+        }
+    }
+}
+
+int grid_for(uint32_t n, int block, int per_sm) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    uint64_t need = (n + (uint64_t)block - 1) / block;
+    uint64_t cap = (uint64_t)sms * per_sm;
+    return (int)(need < cap ? (need ? need : 1) : cap);
+}
+
+}  // namespace crt
+
+using namespace crt;
+
+extern "C" {
+
+int crt_trace_closest(crt_scene s, const float* d_rays, uint32_t n, int32_t* d_index, float* d_t,
+                      float* d_uv, void* stream) {
+    if (!s || (!d_rays && n) || (n && (!d_index || !d_t)))
+        return set_error(CRT_ERR_INVALID, "crt_trace_closest: null argument");
+    if (n == 0) return CRT_OK;
+    if (((uintptr_t)d_rays & 15u) != 0) return set_error(CRT_ERR_INVALID, "rays must be 16-byte aligned");
+    trace_closest_kernel<false><<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
+        s->dev, (const float4*)d_rays, n, d_index, d_t, (float2*)d_uv, nullptr, nullptr);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}
+
+int crt_trace_counts(crt_scene s, const float* d_rays, uint32_t n, uint32_t* d_nodes, uint32_t* d_tris,
+                     void* stream) {
+    if (!s || (n && (!d_rays || !d_nodes || !d_tris)))
+        return set_error(CRT_ERR_INVALID, "crt_trace_counts: null argument");
+    if (n == 0) return CRT_OK;
+    if (((uintptr_t)d_rays & 15u) != 0) return set_error(CRT_ERR_INVALID, "rays must be 16-byte aligned");
+    trace_closest_kernel<true><<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
+        s->dev, (const float4*)d_rays, n, nullptr, nullptr, nullptr, d_nodes, d_tris);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}
+
+}  // extern "C"

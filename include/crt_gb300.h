@@ -1,0 +1,224 @@
+/*
+ * crt_gb300.h -- C ABI of the GB300 (sm_103a) path-tracing library.
+ *
+ * Drop-in replacement for CudaRT's GPU render path.  The reference binds its
+ * renderer through the abstract C++ class `Renderer`
+ * (src/include/renderer.h:78-100) and its GPU implementation
+ * `ParallelRenderer` (src/renderer/parallel_renderer.cu); this header exposes
+ * the same operations as plain C functions over opaque handles so that any
+ * host (the C++ shim in cudart_gb300/shim/, ctypes, cgo, JNI) can call them.
+ *
+ * Conventions
+ *  - Every function returns a crt_status; CRT_OK is 0.  On failure the
+ *    message is available from crt_last_error() (thread-local).  Nothing in
+ *    the library calls exit() (the reference's CUDA_CHECK_RETURN does,
+ *    src/include/cuda_error_check.h:9-21).
+ *  - Handles own all device memory they allocate and free it on *_destroy.
+ *  - Pointers named d_* are device pointers; all others are host pointers.
+ *  - Triangle indices are the caller's face order (the order of
+ *    crt_scene_desc.positions), independent of the BVH layout.
+ *  - There is no CPU fallback: without a usable sm_103a GPU the create
+ *    calls fail with CRT_ERR_CUDA.
+ */
+#ifndef CRT_GB300_H
+#define CRT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRT_API_VERSION 1
+
+#if defined(__GNUC__)
+#define CRT_EXPORT __attribute__((visibility("default")))
+#else
+#define CRT_EXPORT
+#endif
+
+typedef enum {
+    CRT_OK = 0,
+    CRT_ERR_INVALID = 1,      /* bad argument or scene description */
+    CRT_ERR_CUDA = 2,         /* CUDA runtime error (message has details) */
+    CRT_ERR_NOMEM = 3,        /* host or device allocation failed */
+    CRT_ERR_UNSUPPORTED = 4,  /* option not available in this build */
+    CRT_ERR_WATCHDOG = 5,     /* a device traversal exceeded its step or stack limit */
+    CRT_ERR_LIMIT = 6         /* a size exceeds a documented maximum */
+} crt_status;
+
+/* refl_t (src/include/material.h:8-15). */
+typedef enum {
+    CRT_BSDF_DIFFUSE = 0,
+    CRT_BSDF_SPECULAR = 1,
+    CRT_BSDF_DIFFSPEC = 2,
+    CRT_BSDF_MICROFACET = 3,
+    CRT_BSDF_REFRACTIVE = 4,
+    CRT_BSDF_EMISSIVE = 5
+} crt_bsdf;
+
+#define CRT_NO_TEXTURE (-1)
+
+/* One material with the values of its MTL entry; replaces the reference's
+ * Material (src/include/material.h:17-55) as produced by materialFromMtl
+ * (src/geometry/scene.cpp:175-190).  `ka` is the MTL Ka: the library applies
+ * the reference's emission scaling Ka * 3 * (total light area)
+ * (scene.cpp:19,163,177). */
+typedef struct {
+    int32_t bsdf;        /* crt_bsdf */
+    int32_t texture;     /* index into the scene's textures or CRT_NO_TEXTURE */
+    float kd[3];
+    float ka[3];
+    float ks[3];
+    float ns;
+    float ni;            /* index of refraction for CRT_BSDF_REFRACTIVE */
+    float diffuse;       /* diffuse probability for CRT_BSDF_DIFFSPEC */
+} crt_material;
+
+/* Camera (src/include/camera.h:9-22), already derived from the JSON file. */
+typedef struct {
+    float eye[3];
+    float dir[3];
+    float up[3];
+    float right[3];
+    float fov;           /* tan(vertical fov / 2) */
+    float aspect;
+    float aperture;      /* focalLength / fStop; 0 for a pinhole */
+    float focus;         /* |viewDirection| */
+    int32_t xpixels;
+    int32_t ypixels;
+} crt_camera;
+
+/* Scene description: everything Scene::loadTriangles, constructLightList and
+ * TextureStore produce (scene.cpp:74-165, texture_store.cpp:18-71). */
+typedef struct {
+    uint32_t num_triangles;
+    const float* positions;        /* [n][3 vertices][xyz] */
+    const float* normals;          /* [n][3 vertices][xyz] shading normals */
+    const float* uvs;              /* [n][3 vertices][uv]; may be NULL (all 0) */
+    const uint32_t* material_ids;  /* [n] */
+    uint32_t num_materials;
+    const crt_material* materials;
+    uint32_t num_lights;           /* 0: every triangle whose material is
+                                      CRT_BSDF_EMISSIVE, in face order */
+    const uint32_t* light_indices; /* [num_lights] face indices in pick order */
+    uint32_t num_textures;
+    const uint32_t* texture_dims;  /* [num_textures][width, height] */
+    const float* texels;           /* [sum(w*h)][rgb] linear floats, as
+                                      stbi_loadf returns them */
+} crt_scene_desc;
+
+typedef struct crt_scene_s* crt_scene;
+typedef struct crt_render_s* crt_render;
+
+/* Build-time statistics of a scene's BVH and buffers. */
+typedef struct {
+    uint32_t num_triangles;
+    uint32_t num_nodes;        /* 8-wide nodes (80 bytes each) */
+    uint32_t max_depth;        /* levels from the root to the deepest leaf */
+    uint32_t num_lights;
+    uint32_t num_materials;
+    uint32_t num_textures;
+    uint64_t node_bytes;
+    uint64_t triangle_bytes;   /* intersection records (48 bytes each) */
+    uint64_t shading_bytes;    /* normals/uv/material records */
+    uint64_t texture_bytes;
+    float lights_area;
+    float build_ms;
+} crt_scene_info;
+
+/* ---- version / errors ------------------------------------------------ */
+CRT_EXPORT int crt_api_version(void);
+CRT_EXPORT const char* crt_last_error(void);
+
+/* ---- camera -------------------------------------------------------------
+ * CameraJsonLoader::getCamera (src/context/json_loader.cpp:26-48): fov from
+ * `fieldOfView` degrees, aperture = focalLength / fStop, focus = |viewDirection|. */
+CRT_EXPORT int crt_camera_from_json(float fov_deg, float focal_length, float fstop, const float eye[3],
+                         const float view_dir[3], const float up[3], uint32_t width,
+                         uint32_t height, crt_camera* out);
+
+/* ---- scene --------------------------------------------------------------
+ * Replaces Scene::constructBvh + constructLightList (scene.cpp:140-165) and
+ * the uploads in the ParallelRenderer constructor
+ * (parallel_renderer.cu:37-126): builds an 8-wide BVH with quantised child
+ * bounds on the host and uploads it with the triangle, shading, material,
+ * light and texture buffers to the current device. */
+CRT_EXPORT int crt_scene_create(const crt_scene_desc* desc, crt_scene* out);
+CRT_EXPORT int crt_scene_destroy(crt_scene scene);
+CRT_EXPORT int crt_scene_get_info(crt_scene scene, crt_scene_info* out);
+/* Host copies of the BVH as uploaded: nodes [num_nodes][80 bytes],
+ * triangle records [num_triangles][48 bytes] (v1.xyz + face index bits,
+ * e1.xyz + 0, e2.xyz + 0).  Either pointer may be NULL. */
+CRT_EXPORT int crt_scene_export_bvh(crt_scene scene, void* nodes, void* triangles);
+/* The same BVH build on the host alone, without a device (inspection and
+ * build statistics): call once with nodes/triangles NULL to learn
+ * num_nodes, then again with buffers of num_nodes*80 and n*48 bytes.
+ * Replaces constructBVH (src/geometry/bvh.cpp:65-77). */
+CRT_EXPORT int crt_bvh_build_host(const float* positions, uint32_t num_triangles, uint32_t* num_nodes,
+                       uint32_t* max_depth, void* nodes, void* triangles);
+
+/* ---- ray queries ---------------------------------------------------------
+ * Closest hit of a batch of rays; replaces intersectBVH
+ * (src/renderer/renderer.cu:283-330) with Triangle::intersect
+ * (src/geometry/geometry.cu:38-65).  d_rays: [n][8] floats
+ * (o.x o.y o.z tmin d.x d.y d.z tmax).  A hit is the smallest t with
+ * tmin < t < tmax; equal t goes to the lowest face index.  d_index gets the
+ * face index or -1, d_t the distance (FLT_MAX on a miss), d_uv (optional)
+ * the barycentrics.  Asynchronous on `stream` (NULL = default stream). */
+CRT_EXPORT int crt_trace_closest(crt_scene scene, const float* d_rays, uint32_t n, int32_t* d_index,
+                      float* d_t, float* d_uv, void* stream);
+/* Node visits and triangle tests of each ray of crt_trace_closest
+ * (instrumented traversal for the memory roofline). */
+CRT_EXPORT int crt_trace_counts(crt_scene scene, const float* d_rays, uint32_t n, uint32_t* d_nodes,
+                     uint32_t* d_tris, void* stream);
+
+/* ---- progressive render -------------------------------------------------
+ * Replaces ParallelRenderer (src/include/renderer.h:102-126). */
+typedef enum {
+    CRT_MODE_MEGAKERNEL = 0,   /* one kernel per pass runs whole paths */
+    CRT_MODE_WAVEFRONT = 1     /* generate / extend / shade / shadow queues */
+} crt_mode;
+
+typedef struct {
+    uint32_t max_depth;        /* bounces per path; the reference hard-codes 6
+                                  (renderer.cu:25,33) */
+    uint64_t seed;             /* Philox key */
+    uint32_t view_id;          /* Philox counter word: separates views */
+    uint32_t mode;             /* crt_mode */
+    uint32_t block_size;       /* 0 = library default */
+    uint32_t wave_paths;       /* wavefront: paths in flight, 0 = default */
+} crt_render_options;
+
+CRT_EXPORT void crt_render_options_default(crt_render_options* opts);
+
+/* Constructor `ParallelRenderer(scene, w, h, spp)` (parallel_renderer.cu:37-77);
+ * the accumulator starts at zero (the reference leaves it uninitialised). */
+CRT_EXPORT int crt_render_create(crt_scene scene, const crt_camera* camera, uint32_t width,
+                      uint32_t height, const crt_render_options* opts, crt_render* out);
+CRT_EXPORT int crt_render_destroy(crt_render r);
+/* Render n_spp more samples per pixel: n_spp calls of
+ * renderOneSamplePerPixel (parallel_renderer.cu:288-301).  Asynchronous. */
+CRT_EXPORT int crt_render_pass(crt_render r, uint32_t n_spp);
+CRT_EXPORT int crt_render_samples_rendered(crt_render r, uint32_t* out);
+CRT_EXPORT int crt_render_synchronize(crt_render r);
+/* copyImageBytes (parallel_renderer.cu:303-310): RGBA8 of the average with
+ * float3ToUchar4 (renderer.h:149-156) then gammaCorrectPixel
+ * (renderer.cu:495-504); host_rgba holds width*height*4 bytes. */
+CRT_EXPORT int crt_render_resolve(crt_render r, uint8_t* host_rgba);
+/* FP32 per-pixel radiance sums [width*height][3] (host copy). */
+CRT_EXPORT int crt_render_accum(crt_render r, float* host_rgb);
+/* Device pointer of the accumulator, valid until destroy. */
+CRT_EXPORT int crt_render_accum_device(crt_render r, float** d_rgb);
+CRT_EXPORT int crt_render_reset(crt_render r);
+CRT_EXPORT int crt_render_set_camera(crt_render r, const crt_camera* camera);
+/* Use the caller's CUDA stream (cudaStream_t) instead of the handle's own. */
+CRT_EXPORT int crt_render_set_stream(crt_render r, void* stream);
+/* Extension and shadow rays traced by the passes since the last reset. */
+CRT_EXPORT int crt_render_ray_counts(crt_render r, uint64_t* extension_rays, uint64_t* shadow_rays);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

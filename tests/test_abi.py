@@ -1,0 +1,105 @@
+"""The C ABI library loads, exports every symbol include/crt_gb300.h
+declares, and rejects bad scene descriptions with status codes (host-side
+validation runs before any device call, so these need no GPU)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from cudart_gb300 import _lib, scenes
+from cudart_gb300._lib import CrtError
+
+HEADER = os.path.join(ROOT, "include", "crt_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"CRT_EXPORT\s+[\w\s\*]+?\b(crt_\w+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported():
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    lib = _lib.load()
+    for s in syms:
+        assert hasattr(lib, s), s
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (crt_\w+)", out))
+    assert exported == set(syms), exported ^ set(syms)
+    assert set(_lib.SIGNATURES) == set(syms)
+
+
+def test_api_version():
+    assert _lib.load().crt_api_version() == 1
+
+
+def _desc(sc, **over):
+    pos = np.ascontiguousarray(sc.positions, np.float32)
+    nor = np.ascontiguousarray(sc.normals, np.float32)
+    mid = np.ascontiguousarray(sc.material_ids, np.uint32)
+    mats = (_lib.Material * len(sc.materials))()
+    for i, m in enumerate(sc.materials):
+        mats[i].bsdf, mats[i].texture = m.bsdf, m.tex
+        mats[i].kd[:] = list(m.kd)
+        mats[i].ka[:] = list(m.ka)
+    keep = [pos, nor, mid, mats]
+    d = dict(num_triangles=sc.n_tris, positions=pos.ctypes.data, normals=nor.ctypes.data, uvs=None,
+             material_ids=mid.ctypes.data, num_materials=len(sc.materials), materials=C.addressof(mats),
+             num_lights=0, light_indices=None, num_textures=0, texture_dims=None, texels=None)
+    d.update(over)
+    return _lib.SceneDesc(**d), keep
+
+
+def _create(desc):
+    h = C.c_void_p()
+    st = _lib.load().crt_scene_create(C.byref(desc), C.byref(h))
+    return st, _lib.load().crt_last_error().decode()
+
+
+def test_scene_without_lights_is_rejected():
+    sc = scenes.cornell_box()
+    sc.materials[3].bsdf = scenes.DIFFUSE          # the light quad stops emitting
+    desc, keep = _desc(sc)
+    st, msg = _create(desc)
+    assert st == 1 and "emissive" in msg
+
+
+def test_bad_material_index_is_rejected():
+    sc = scenes.cornell_box()
+    sc.material_ids = sc.material_ids.copy()
+    sc.material_ids[5] = 99
+    desc, keep = _desc(sc)
+    st, msg = _create(desc)
+    assert st == 1 and "material id" in msg
+
+
+def test_bad_texture_index_is_rejected():
+    sc = scenes.cornell_box()
+    sc.materials[0].tex = 3
+    desc, keep = _desc(sc)
+    st, msg = _create(desc)
+    assert st == 1 and "texture" in msg
+
+
+def test_empty_scene_and_null_args_are_rejected():
+    sc = scenes.cornell_box()
+    desc, keep = _desc(sc, num_triangles=0)
+    assert _create(desc)[0] == 1
+    assert _lib.load().crt_scene_create(None, None) == 1
+    assert _lib.load().crt_trace_closest(None, None, 0, None, None, None, None) == 1
+    with pytest.raises(CrtError):
+        _lib.check(1)
+
+
+def test_camera_from_json_matches_oracle():
+    import oracle
+    from cudart_gb300 import camera_from_json
+    for spec, (w, h) in [(scenes.CORNELL_CAMERA, (512, 512)), (scenes.large_textured.__defaults__ and
+                          scenes.CameraSpec(45.0, (0, 3.2, 7.5), (0, -3.2, -7.5)), (1920, 1080))]:
+        c = camera_from_json(spec, w, h)
+        o = oracle.make_camera(spec, w, h)
+        assert bytes(c) == o.tobytes()
