@@ -1,0 +1,353 @@
+"""Benchmark: Msamples/s of the 1080p textured-heightfield workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (seeded synthetic data, see cudart_gb300/scenes.py large_textured):
+1024x1024-vertex heightfield (~2.09M triangles) with a 1024^2 RGBA8 texture,
+64 glass/mirror icospheres, 4 quad lights; 1920x1080, 256 samples per pixel,
+max depth 8.  One step renders the whole frame (531M path samples).
+
+* value: wavefront form, device time (CUDA events on the render stream),
+  scene resident in HBM; L2 flushed (256 MiB write) before every step.
+* plain_kernel: the drop-in megakernel on the same frame; its accumulator
+  must equal the wavefront's bit for bit (equal RMSE by construction).
+* e2e: the public API from host arrays to host image: crt_scene_create
+  (BVH build + uploads) + crt_render_create + crt_render_pass +
+  crt_render_resolve, wall clock.
+* roofline: the dominant stage of a profiled pass (per-launch CUDA events,
+  node and triangle fetches counted by an untimed re-run) against the
+  measured HBM copy bandwidth.
+* cpu_baseline / --impl reference: the CPU oracle port of the reference's
+  `--cpu` path on all host threads over a bounded pixel sample.
+
+Under torchrun each rank renders its own sample range of the same frame
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s at 1080p, equal RMSE, vs plain kernel; adjoint/forward time ratio"
+WORKLOAD = ("large_textured 1920x1080 256spp depth8: 1024^2-vertex heightfield + 1024^2 RGBA8 "
+            "texture, 64 glass/mirror icospheres (subdiv 3), 4 quad lights, 2,174,986 triangles")
+NODE_BYTES, TRI_BYTES = 80, 48
+L2_FLUSH_BYTES = 256 << 20
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def cpu_port_sample(sc, seconds: float, threads: int):
+    """Oracle port (restatement of the reference's --cpu path) and a bounded
+    sample of the frame sized to about `seconds` of work on `threads`:
+    a stratified pixel subset at 1 spp, or the whole frame at k spp.
+    Returns (scene, camera, pixels, spp)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+    oracle.build()
+    o = oracle.OracleScene(sc)
+    cam = oracle.make_camera(sc.camera, sc.width, sc.height)
+    npix = sc.width * sc.height
+    probe = (np.arange(4096, dtype=np.uint64) * (npix // 4096) % npix).astype(np.uint32)
+    t = time.perf_counter()
+    o.render(cam, 7, 1, sc.max_depth, pixels=probe, threads=threads)
+    rate = len(probe) / max(time.perf_counter() - t, 1e-6)
+    target = max(4096.0, rate * seconds)
+    if target <= npix:
+        n = int(target)
+        px = (np.arange(n, dtype=np.uint64) * (npix // n) % npix).astype(np.uint32)
+        return o, cam, px, 1
+    return o, cam, None, int(round(target / npix))
+
+
+def run_reference(args):
+    """--impl reference: the CPU path timed on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from cudart_gb300 import scenes
+    threads = os.cpu_count() or 1
+    sc = scenes.large_textured()
+    o, cam, px, k_spp = cpu_port_sample(sc, 5.0, threads)
+    n_samples = (len(px) if px is not None else sc.width * sc.height) * k_spp
+    times = []
+    for k in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        o.render(cam, 1234, k_spp, sc.max_depth, pixels=px, spp0=k * k_spp, threads=threads)
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t)
+    dt = sum(times)
+    value = n_samples * args.steps / dt / 1e6
+    sample = (f"{n_samples} samples per step: "
+              + (f"{len(px)} stratified pixels x 1 spp" if px is not None else f"full frame x {k_spp} spp")
+              + " of the 1920x1080 frame")
+    print(json.dumps({
+        "metric": METRIC, "value": round(value, 5), "unit": "Msamples/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+        "config": {"workload": WORKLOAD, "path": "CPU restatement of the reference --cpu path, OpenMP"},
+        "cpu_baseline": {"value": round(value, 5), "unit": "Msamples/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 5), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    from cudart_gb300 import GB300Renderer, GB300Scene, scenes
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    spp = args.spp
+    sc = scenes.large_textured(spp=spp) if not args.small else scenes.large_textured(
+        width=480, height=270, spp=spp, grid=256, tex_size=256, n_spheres=16)
+    npix = sc.width * sc.height
+    # one non-default stream carries the renders, the L2 flushes and the events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    scene = GB300Scene(sc)
+    info = scene.info
+    # each rank renders its own Philox streams of the same frame (view_id = rank)
+    wf = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
+                       mode="wavefront", view_id=rank)
+    wf.set_stream(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timed_steps(r, k_steps):
+        durs = []
+        for k in range(k_steps):
+            flush.fill_(float(k))
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            r.reset()
+            s.record(stream)
+            r.render(spp)
+            e.record(stream)
+            durs.append((s, e))
+        torch.cuda.synchronize()
+        return [s.elapsed_time(e) for s, e in durs]
+
+    for _ in range(args.warmup):
+        wf.reset()
+        wf.render(spp)
+    barrier()
+    with ClockSampler(local) as clk:
+        barrier()
+        ms = timed_steps(wf, args.steps)
+        barrier()
+    clocks = clk.summary()
+    ms_step = sum(ms) / len(ms)
+    if dist is not None:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * npix * spp / (ms_step * 1e-3) / 1e6
+    ext, shd = wf.ray_counts()          # counters restart at every reset: last step only
+    rays_per_sample = (ext + shd) / (npix * spp)
+    wf_acc = wf.accum()
+
+    # plain drop-in megakernel on the same frame
+    mk = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
+                       mode="megakernel", view_id=rank)
+    mk.set_stream(stream.cuda_stream)
+    mk.reset()
+    mk.render(spp)
+    torch.cuda.synchronize()
+    k_plain = max(1, min(args.steps, 2))
+    mk_ms = sum(timed_steps(mk, k_plain)) / k_plain
+    identical = bool(np.array_equal(mk.accum(), wf_acc))
+    plain_value = npix * spp / (mk_ms * 1e-3) / 1e6
+
+    out = None
+    if rank == 0:
+        # roofline: profiled pass of 8 spp (per-launch events, counted fetches)
+        prof_r = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
+                               mode="wavefront")
+        prof_r.set_stream(stream.cuda_stream)
+        prof = prof_r.profile_pass(8)
+        stages = ("generate", "extend", "shade", "shadow", "accumulate", "bookkeeping")
+        dom = max(stages, key=lambda s: prof[f"{s}_ms"])
+        peak, peak_kind = measured_peaks()
+        roof = {}
+        for stage, rays, nodes, tris in (("extend", "extension_rays", "extension_nodes", "extension_tris"),
+                                         ("shadow", "shadow_rays", "shadow_nodes", "shadow_tris")):
+            launches = prof[f"{stage}_launches"]
+            alg = prof[nodes] * NODE_BYTES + prof[tris] * TRI_BYTES
+            ms_l = prof[f"{stage}_ms"] / launches
+            gbs = alg / launches / (ms_l * 1e-3) / 1e9
+            roof[stage] = {"kernel": "wf_" + stage, "bytes_per_launch": alg / launches,
+                           "ms_per_launch": ms_l, "gbs": gbs, "rays": prof[rays],
+                           "nodes_per_ray": prof[nodes] / max(prof[rays], 1),
+                           "tris_per_ray": prof[tris] / max(prof[rays], 1)}
+        main = roof["extend"] if dom != "shadow" else roof["shadow"]
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic_per_ray.json")
+        if os.path.exists(tp):
+            tr = json.load(open(tp)).get(main["kernel"])
+            if tr:
+                traffic = tr["dram_bytes_per_ray"] * main["rays"] / prof[f"{dom if dom in roof else 'extend'}_launches"]
+        roofline = {"bound": "hbm", "kernel": main["kernel"], "achieved": round(main["gbs"], 1),
+                    "peak": peak, "unit": "GB/s", "frac": round(main["gbs"] / peak, 4),
+                    "traffic": traffic, "peak_kind": f"{peak_kind} (HBM copy)",
+                    "algorithmic_bytes": "nodes visited x 80 B + triangles tested x 48 B per ray",
+                    "stage_ms": {s: round(prof[f"{s}_ms"], 2) for s in stages},
+                    "stages": {k: {kk: (round(vv, 3) if isinstance(vv, float) else vv)
+                                   for kk, vv in v.items()} for k, v in roof.items()}}
+        del prof_r
+
+        # e2e: host arrays -> host image through the public API
+        h2d = int(info.node_bytes + info.triangle_bytes + info.shading_bytes + info.texture_bytes)
+        e2e_t = []
+        for k in range(1 + max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s2 = GB300Scene(sc)
+            r2 = GB300Renderer(s2, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
+                               mode="wavefront")
+            r2.render(spp)
+            img = r2.copy_image_bytes()
+            e2e_t.append(time.perf_counter() - t0)
+            del r2, s2
+        e2e_s = statistics.mean(e2e_t[1:])
+        e2e = {"value": round(npix * spp / e2e_s / 1e6, 3), "unit": "Msamples/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(img.nbytes),
+               "seconds_per_step": round(e2e_s, 4),
+               "region": "crt_scene_create (host BVH build + uploads) + crt_render_create + "
+                         "crt_render_pass(256) + crt_render_resolve to host RGBA8"}
+
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            threads = os.cpu_count() or 1
+            o, cam, px, k_spp = cpu_port_sample(sc, 12.0, threads)
+            n_samples = (len(px) if px is not None else npix) * k_spp
+            t0 = time.perf_counter()
+            o.render(cam, 1234, k_spp, sc.max_depth, pixels=px, threads=threads)
+            dt = time.perf_counter() - t0
+            cpu = {"value": round(n_samples / dt / 1e6, 5), "unit": "Msamples/s", "cores": threads,
+                   "kind": "port",
+                   "sample": (f"{len(px)} stratified pixels x 1 spp" if px is not None
+                              else f"full frame x {k_spp} spp") + f" of the 1920x1080 frame, {dt:.1f} s"}
+        waves = math.ceil(spp / max(1, (1 << 22) // npix)) if npix <= (1 << 22) else spp * math.ceil(npix / (1 << 22))
+        launches = args.steps * waves * (3 + 4 * sc.max_depth)
+        out = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator: heightfield value noise, procedural texture)",
+            "config": {"workload": WORKLOAD, "mode": "wavefront (CUDA-graph waves of 4M paths)",
+                       "width": sc.width, "height": sc.height, "spp": spp, "max_depth": sc.max_depth,
+                       "triangles": info.num_triangles, "bvh_nodes": info.num_nodes,
+                       "bvh_depth": info.max_depth,
+                       "l2": "flushed before every step (256 MiB write); scene buffers > L2"},
+            "plain_kernel": {"value": round(plain_value, 3), "ms_per_step": round(mk_ms, 3),
+                             "accum_identical_to_wavefront": identical},
+            "speedup_vs_plain": round(value / world / plain_value, 3),
+            "mrays_per_s": round(value * rays_per_sample, 1),
+            "rays_per_sample": round(rays_per_sample, 3),
+            "adjoint_forward_ratio": None,
+            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--spp", type=int, default=256)
+    ap.add_argument("--small", action="store_true", help="480x270 reduced scene (profiling)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -45,7 +45,11 @@ class SceneDesc(C.Structure):
                 ("num_materials", C.c_uint32), ("materials", C.c_void_p),
                 ("num_lights", C.c_uint32), ("light_indices", C.c_void_p),
                 ("num_textures", C.c_uint32), ("texture_dims", C.c_void_p),
-                ("texels", C.c_void_p)]
+                ("texels", C.c_void_p), ("node_format", C.c_uint32)]
+
+
+NODES_Q8 = 0
+NODES_F32 = 1
 
 
 class SceneInfo(C.Structure):
@@ -57,9 +61,22 @@ class SceneInfo(C.Structure):
                 ("lights_area", C.c_float), ("build_ms", C.c_float)]
 
 
+class StageProfile(C.Structure):
+    STAGES = ("generate", "extend", "shade", "shadow", "accumulate", "bookkeeping")
+    _fields_ = [("ms", C.c_double * 6), ("launches", C.c_uint64 * 6),
+                ("extension_rays", C.c_uint64), ("extension_nodes", C.c_uint64),
+                ("extension_tris", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("shadow_nodes", C.c_uint64), ("shadow_tris", C.c_uint64)]
+
+
 class RenderOptions(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("seed", C.c_uint64), ("view_id", C.c_uint32),
-                ("mode", C.c_uint32), ("block_size", C.c_uint32), ("wave_paths", C.c_uint32)]
+                ("mode", C.c_uint32), ("block_size", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+FLAG_LANE_REFILL = 1
+FLAG_SPLIT_LEAF = 2
 
 
 # name -> (restype, argtypes); every entry point of include/crt_gb300.h
@@ -88,6 +105,7 @@ SIGNATURES = {
     "crt_render_set_camera": (C.c_int, [P, P]),
     "crt_render_set_stream": (C.c_int, [P, P]),
     "crt_render_ray_counts": (C.c_int, [P, P, P]),
+    "crt_render_profile_pass": (C.c_int, [P, U32, P]),
 }
 
 _lib = None

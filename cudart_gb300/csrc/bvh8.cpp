@@ -201,6 +201,8 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
     out.tris.reserve(n);
     out.max_depth = 0;
     out.margin = margin;
+    out.fnodes.clear();
+    out.fnodes_ok = true;
     out.nodes.resize(1);
     for (size_t qi = 0; qi < queue.size(); ++qi) {
         const Item it = queue[qi];
@@ -259,6 +261,8 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
 
         Bvh8Node node;
         std::memset(&node, 0, sizeof(node));
+        Bvh8FloatNode fnode;
+        std::memset(&fnode, 0, sizeof(fnode));
         node.px = nb.lo[0];
         node.py = nb.lo[1];
         node.pz = nb.lo[2];
@@ -272,8 +276,21 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
         uint32_t tri_off = 0;
         for (int s = 0; s < 8; ++s) {
             int32_t c = child_at[s];
-            if (c < 0) continue;
+            if (c < 0) {
+                // empty slot: inverted box (lo plane above hi plane) never hits
+                for (int k = 0; k < 3; ++k) {
+                    node.qlo[k][s] = 255;
+                    node.qhi[k][s] = 0;
+                    fnode.lo[k][s] = FLT_MAX;
+                    fnode.hi[k][s] = -FLT_MAX;
+                }
+                continue;
+            }
             const Node2& cn = n2[c];
+            for (int k = 0; k < 3; ++k) {
+                fnode.lo[k][s] = cn.box.lo[k];
+                fnode.hi[k][s] = cn.box.hi[k];
+            }
             for (int k = 0; k < 3; ++k) {
                 double step = std::ldexp(1.0, e[k]);
                 double lo = std::floor(((double)cn.box.lo[k] - (double)nb.lo[k]) / step);
@@ -304,6 +321,12 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
         }
         out.nodes.resize(out.nodes.size() + __builtin_popcount(node.imask));
         out.nodes[qi] = node;
+        if (node.child_base >= (1u << 24)) out.fnodes_ok = false;   // 24-bit child index
+        fnode.child_base_imask = node.child_base | ((uint32_t)node.imask << 24);
+        fnode.tri_base = node.tri_base;
+        std::memcpy(fnode.meta, node.meta, 8);
+        out.fnodes.resize(out.nodes.size());
+        out.fnodes[qi] = fnode;
     }
     *msg = nullptr;
     return true;

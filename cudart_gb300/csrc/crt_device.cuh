@@ -35,7 +35,8 @@ enum ErrorBits : uint32_t { ERR_WATCHDOG = 1u, ERR_STACK = 2u };
 // Device view of a scene (all arrays in HBM, 16-byte aligned).
 // ---------------------------------------------------------------------------
 struct DevScene {
-    const float4* nodes;       // 5 float4 per 8-wide node
+    const float4* nodes;       // 5 float4 per 8-wide node (8-bit quantised planes)
+    const float4* fnodes;      // 13 float4 per node with FP32 planes, or null
     const float4* tris;        // 3 float4 per record (leaf order)
     const float4* shade;       // 3 float4 per face: n1.xyz n2.x | n2.yz n3.xy | n3.z area mat 0
     const float4* uvs;         // 2 float4 per face: uv1 uv2 | uv3 0 0
@@ -183,44 +184,120 @@ CRT_D float safe_rcp(float d) {
     return 1.0f / copysignf(a > 0x1p-80f ? a : 0x1p-80f, d);
 }
 
+// Three-input min / max (PTX ISA 8.8, sm_100 and later): one instruction each.
+CRT_D float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+CRT_D float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Bit s of m moves to bit s ^ oct (8-bit masks).
+CRT_D uint32_t permute_octant(uint32_t m, uint32_t oct) {
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m & 0xAAu) >> 1);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m & 0xCCu) >> 2);
+    if (oct & 4u) m = ((m & 0x0Fu) << 4) | ((m & 0xF0u) >> 4);
+    return m;
+}
+
 CRT_D float byte_as_float(uint32_t word, uint32_t sel) {
     // 0x4B0000bb is 2^23 + bb; subtracting 2^23 gives bb exactly.
     return __uint_as_float(__byte_perm(word, 0x4B000000u, sel)) - 8388608.0f;
 }
 
-// Mode CLOSEST: nearest hit with lowest-face tie rule, h.t starts at tmax.
-// Mode OCCLUDED: returns true as soon as a face other than `target` is hit
-// with t < h.t, or t == h.t and face < target (exactly the faces that
-// would make the closest hit differ from `target`).
-template <bool OCCLUDED, bool COUNT>
-CRT_D bool traverse(const DevScene& S, float3 o, float3 d, float tmin, Hit& h, int32_t target,
-                    Stack& st, TraversalStats* stats) {
-    const float ix = safe_rcp(d.x), iy = safe_rcp(d.y), iz = safe_rcp(d.z);
-    const uint32_t oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
-    // near/far plane selection per axis: negative direction enters at the hi plane
-    const bool nx = oct & 1u, ny = oct & 2u, nz = oct & 4u;
-    uint2 grp = make_uint2(0u, ((1u << oct) << 8) | 1u);   // root = slot 0 of a virtual parent
-    st.sp = 0;
-    uint32_t visits = 0;
-    for (;;) {
-        uint32_t hits = grp.y >> 8;
-        if (hits == 0) {
-            if (st.sp == 0) break;
-            grp = st.pop();
-            continue;
-        }
-        const uint32_t k = __ffs(hits) - 1;
-        hits &= hits - 1;
-        const uint32_t imask = grp.y & 0xFFu;
-        const uint32_t slot = k ^ oct;
-        const uint32_t node = grp.x + __popc(imask & ((1u << slot) - 1u));
-        if (hits) {
-            if (st.sp >= kMaxLevels) { atomicOr(S.error, ERR_STACK); break; }
-            st.push(make_uint2(grp.x, (hits << 8) | imask));
-        }
-        if (++visits > kMaxNodeVisits) { atomicOr(S.error, ERR_WATCHDOG); break; }
-        if (COUNT) stats->nodes++;
+// Resumable traversal of one ray.  step() visits one node (popping the
+// stack first when the current group is exhausted) and tests the triangles
+// of the leaves it hits; it returns true when the ray is finished.  Kernels
+// that keep a lane busy with a new ray as soon as its old one finishes drive
+// step() directly; traverse() runs a ray to completion.
+//
+// Mode CLOSEST: nearest hit with the lowest-face tie rule, h.t starts at tmax.
+// Mode OCCLUDED: finishes as soon as a face other than `target` is hit with
+// t < h.t, or t == h.t and face < target (exactly the faces that would make
+// the closest hit differ from `target`); `occluded` is then true.
+template <bool OCCLUDED, bool COUNT, bool WHOLE_LEAF = true, bool F32 = false>
+struct Traversal {
+    float3 o, d;
+    float ix, iy, iz, tmin;
+    uint32_t oct;
+    uint2 grp;          // child base, (visit-order hit mask << 8) | internal mask
+    uint32_t tri_base;  // triangles of the last visited node still to test
+    uint32_t tri_mask;
+    uint32_t visits;
+    int32_t target;
+    bool occluded;
+    Hit h;
 
+    CRT_D void init(float3 o_, float3 d_, float tmin_, float tmax, int32_t target_, Stack& st) {
+        o = o_;
+        d = d_;
+        ix = safe_rcp(d.x);
+        iy = safe_rcp(d.y);
+        iz = safe_rcp(d.z);
+        tmin = tmin_;
+        oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
+        grp = make_uint2(0u, ((1u << oct) << 8) | 1u);   // root = slot 0 of a virtual parent
+        tri_base = tri_mask = 0;
+        visits = 0;
+        target = target_;
+        occluded = false;
+        h.t = tmax;
+        h.face = -1;
+        h.u = h.v = 0.f;
+        st.sp = 0;
+    }
+
+    // One pending triangle test.  Returns true if it ends an occlusion query.
+    CRT_D bool test_triangle(const DevScene& S, TraversalStats* stats) {
+        const uint32_t b = __ffs(tri_mask) - 1;
+        tri_mask &= tri_mask - 1;
+        const float4* tp = S.tris + 3ull * (tri_base + b);
+        const float4 a = ldg(tp), e1 = ldg(tp + 1), e2 = ldg(tp + 2);
+        if (COUNT) stats->tris++;
+        float u, v;
+        const float t = mt_intersect(o, d, xyz(a), xyz(e1), xyz(e2), u, v);
+        const int32_t face = (int32_t)__float_as_uint(a.w);
+        if (t == FLT_MAX || !(t > tmin)) return false;
+        if (OCCLUDED) {
+            if (face != target && (t < h.t || (t == h.t && face < target))) {
+                occluded = true;
+                return true;
+            }
+        } else if (t < h.t || (t == h.t && h.face >= 0 && face < h.face)) {
+            h.t = t;
+            h.face = face;
+            h.u = u;
+            h.v = v;
+        }
+        return false;
+    }
+
+    // One unit of work: the next pending triangle of the last visited node,
+    // else one node visit.  Lanes of a warp that are testing triangles and
+    // lanes that are visiting nodes each do one unit per step, so a leaf
+    // with many triangles does not hold the other lanes back.
+    // With WHOLE_LEAF a step is one node visit followed by all of its
+    // triangle tests.
+    CRT_D bool step(const DevScene& S, Stack& st, TraversalStats* stats) {
+        if (WHOLE_LEAF) {
+            if (visit(S, st, stats)) return true;
+            while (tri_mask)
+                if (test_triangle(S, stats)) return true;
+            return false;
+        }
+        if (tri_mask) return test_triangle(S, stats);
+        return visit(S, st, stats);
+    }
+
+    // Slab tests of the 8 children of an 80-byte node: planes are 8-bit
+    // offsets from the node origin in units of a power-of-two scale.
+    CRT_D void test_children_q8(const DevScene& S, uint32_t node, uint32_t& child_base, uint32_t& child_imask,
+                                uint32_t& tri_base_new, uint32_t& meta_lo, uint32_t& meta_hi,
+                                uint32_t& hitmask) const {
         const float4* np = S.nodes + 5ull * node;
         const float4 n0 = ldg(np), n1 = ldg(np + 1), n2 = ldg(np + 2), n3 = ldg(np + 3), n4 = ldg(np + 4);
         const uint32_t ebits = __float_as_uint(n0.w);
@@ -228,10 +305,14 @@ CRT_D bool traverse(const DevScene& S, float3 o, float3 d, float tmin, Hit& h, i
         const float sy = __uint_as_float(((ebits >> 8) & 0xFFu) << 23) * iy;
         const float sz = __uint_as_float(((ebits >> 16) & 0xFFu) << 23) * iz;
         const float ax = (n0.x - o.x) * ix, ay = (n0.y - o.y) * iy, az = (n0.z - o.z) * iz;
-        const uint32_t child_imask = ebits >> 24;
-        const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
-        const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
-        // quantised planes: lo x|y|z in n2.xy n2.zw n3.xy, hi x|y|z in n3.zw n4.xy n4.zw
+        child_imask = ebits >> 24;
+        child_base = __float_as_uint(n1.x);
+        tri_base_new = __float_as_uint(n1.y);
+        meta_lo = __float_as_uint(n1.z);
+        meta_hi = __float_as_uint(n1.w);
+        // quantised planes: lo x|y|z in n2.xy n2.zw n3.xy, hi x|y|z in n3.zw n4.xy n4.zw;
+        // a negative direction enters a slab at its hi plane
+        const bool nx = oct & 1u, ny = oct & 2u, nz = oct & 4u;
         const uint32_t nlx0 = __float_as_uint(nx ? n3.z : n2.x), nlx1 = __float_as_uint(nx ? n3.w : n2.y);
         const uint32_t flx0 = __float_as_uint(nx ? n2.x : n3.z), flx1 = __float_as_uint(nx ? n2.y : n3.w);
         const uint32_t nly0 = __float_as_uint(ny ? n4.x : n2.z), nly1 = __float_as_uint(ny ? n4.y : n2.w);
@@ -239,10 +320,9 @@ CRT_D bool traverse(const DevScene& S, float3 o, float3 d, float tmin, Hit& h, i
         const uint32_t nlz0 = __float_as_uint(nz ? n4.z : n3.x), nlz1 = __float_as_uint(nz ? n4.w : n3.y);
         const uint32_t flz0 = __float_as_uint(nz ? n3.x : n4.z), flz1 = __float_as_uint(nz ? n3.y : n4.w);
         const float tfar_cap = h.t;
-        uint32_t child_hits = 0, tri_mask = 0;
+        hitmask = 0;
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
-            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
             const uint32_t sel = (uint32_t)(s & 3) | 0x7540u;
             const float tnx = fmaf(byte_as_float(s < 4 ? nlx0 : nlx1, sel), sx, ax);
             const float tfx = fmaf(byte_as_float(s < 4 ? flx0 : flx1, sel), sx, ax);
@@ -250,36 +330,139 @@ CRT_D bool traverse(const DevScene& S, float3 o, float3 d, float tmin, Hit& h, i
             const float tfy = fmaf(byte_as_float(s < 4 ? fly0 : fly1, sel), sy, ay);
             const float tnz = fmaf(byte_as_float(s < 4 ? nlz0 : nlz1, sel), sz, az);
             const float tfz = fmaf(byte_as_float(s < 4 ? flz0 : flz1, sel), sz, az);
-            const float tnear = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-            const float tfar = fminf(fminf(tfx, tfy), fminf(tfz, tfar_cap));
-            if (meta != 0u && tnear <= tfar) {
-                if (child_imask & (1u << s)) child_hits |= 1u << (s ^ oct);
-                else tri_mask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-            }
+            const float tnear = max3f(tnx, tny, fmaxf(tnz, tmin));
+            const float tfar = min3f(tfx, tfy, fminf(tfz, tfar_cap));
+            hitmask |= (tnear <= tfar ? 1u : 0u) << s;
         }
-        grp = make_uint2(child_base, (child_hits << 8) | child_imask);
-        while (tri_mask) {
-            const uint32_t b = __ffs(tri_mask) - 1;
-            tri_mask &= tri_mask - 1;
-            const float4* tp = S.tris + 3ull * (tri_base + b);
-            const float4 a = ldg(tp), e1 = ldg(tp + 1), e2 = ldg(tp + 2);
-            if (COUNT) stats->tris++;
-            float u, v;
-            const float t = mt_intersect(o, d, xyz(a), xyz(e1), xyz(e2), u, v);
-            const int32_t face = (int32_t)__float_as_uint(a.w);
-            if (t == FLT_MAX || !(t > tmin)) continue;
-            if (OCCLUDED) {
-                if (face != target && (t < h.t || (t == h.t && face < target))) return true;
-            } else if (t < h.t || (t == h.t && h.face >= 0 && face < h.face)) {
-                h.t = t;
-                h.face = face;
-                h.u = u;
-                h.v = v;
+    }
+
+    // Slab tests of the 8 children of a 208-byte node with FP32 planes:
+    // t = plane * (1/d) - o * (1/d) in one fused multiply-add per plane.
+    CRT_D void test_children_f32(const DevScene& S, uint32_t node, uint32_t& child_base, uint32_t& child_imask,
+                                 uint32_t& tri_base_new, uint32_t& meta_lo, uint32_t& meta_hi,
+                                 uint32_t& hitmask) const {
+        const float4* np = S.fnodes + 13ull * node;
+        const float4 hd = ldg(np + 12);
+        const uint32_t cbi = __float_as_uint(hd.x);
+        child_base = cbi & 0xFFFFFFu;
+        child_imask = cbi >> 24;
+        tri_base_new = __float_as_uint(hd.y);
+        meta_lo = __float_as_uint(hd.z);
+        meta_hi = __float_as_uint(hd.w);
+        // planes: lo x, y, z at float4 0-1, 2-3, 4-5; hi x, y, z at 6-7, 8-9, 10-11
+        const int nxo = (oct & 1u) ? 6 : 0, nyo = (oct & 2u) ? 8 : 2, nzo = (oct & 4u) ? 10 : 4;
+        const float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+        const float tfar_cap = h.t;
+        hitmask = 0;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {   // slots 4*half .. 4*half+3
+            const float4 nxv = ldg(np + nxo + half), fxv = ldg(np + (6 - nxo) + half);
+            const float4 nyv = ldg(np + nyo + half), fyv = ldg(np + (10 - nyo) + half);
+            const float4 nzv = ldg(np + nzo + half), fzv = ldg(np + (14 - nzo) + half);
+            const float nxs[4] = {nxv.x, nxv.y, nxv.z, nxv.w}, fxs[4] = {fxv.x, fxv.y, fxv.z, fxv.w};
+            const float nys[4] = {nyv.x, nyv.y, nyv.z, nyv.w}, fys[4] = {fyv.x, fyv.y, fyv.z, fyv.w};
+            const float nzs[4] = {nzv.x, nzv.y, nzv.z, nzv.w}, fzs[4] = {fzv.x, fzv.y, fzv.z, fzv.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float tnear = max3f(fmaf(nxs[j], ix, ox), fmaf(nys[j], iy, oy), fmaxf(fmaf(nzs[j], iz, oz), tmin));
+                const float tfar = min3f(fmaf(fxs[j], ix, ox), fmaf(fys[j], iy, oy), fminf(fmaf(fzs[j], iz, oz), tfar_cap));
+                hitmask |= (tnear <= tfar ? 1u : 0u) << (4 * half + j);
             }
         }
     }
-    return false;
+
+    // Visits the next node: pops the stack first when the current group is
+    // exhausted; returns true when nothing is left.
+    CRT_D bool visit(const DevScene& S, Stack& st, TraversalStats* stats) {
+        uint32_t hits = grp.y >> 8;
+        if (hits == 0) {
+            if (st.sp == 0) return true;
+            grp = st.pop();
+            hits = grp.y >> 8;
+        }
+        const uint32_t k = __ffs(hits) - 1;
+        hits &= hits - 1;
+        const uint32_t imask = grp.y & 0xFFu;
+        const uint32_t slot = k ^ oct;
+        const uint32_t node = grp.x + __popc(imask & ((1u << slot) - 1u));
+        if (hits) {
+            if (st.sp >= kMaxLevels) { atomicOr(S.error, ERR_STACK); return true; }
+            st.push(make_uint2(grp.x, (hits << 8) | imask));
+        }
+        if (++visits > kMaxNodeVisits) { atomicOr(S.error, ERR_WATCHDOG); return true; }
+        if (COUNT) stats->nodes++;
+
+        uint32_t child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask;
+        if (F32) test_children_f32(S, node, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);
+        else test_children_q8(S, node, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);
+        // Empty slots hold inverted boxes and never hit; a leaf's meta byte
+        // gives its triangle count (bits 5-6) and offset (bits 0-4).
+        uint32_t leaves = hitmask & ~child_imask;
+        uint32_t tri_mask_new = 0;
+        while (leaves) {
+            const uint32_t s = __ffs(leaves) - 1;
+            leaves &= leaves - 1;
+            const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xFFu;
+            tri_mask_new |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+        }
+        const uint32_t child_hits = permute_octant(hitmask & child_imask, oct);
+        grp = make_uint2(child_base, (child_hits << 8) | child_imask);
+        tri_base = tri_base_new;
+        tri_mask = tri_mask_new;
+        return false;
+    }
+};
+
+template <bool OCCLUDED, bool COUNT, bool F32 = false>
+CRT_D bool traverse(const DevScene& S, float3 o, float3 d, float tmin, Hit& h, int32_t target,
+                    Stack& st, TraversalStats* stats) {
+    Traversal<OCCLUDED, COUNT, true, F32> T;
+    T.init(o, d, tmin, h.t, target, st);
+    while (!T.step(S, st, stats)) {
+    }
+    if (!OCCLUDED) h = T.h;
+    return T.occluded;
 }
+
+// Warp-local pool of queue entries for persistent kernels: lanes whose ray
+// finished take the next entries at once, and the warp claims 32 more from
+// the global counter only when the pool runs dry.
+struct WarpPool {
+    uint32_t next, end;      // warp-uniform
+    bool exhausted;
+
+    CRT_D void init() { next = end = 0; exhausted = false; }
+
+    // Returns the queue index for this lane (or UINT32_MAX) when `want`.
+    CRT_D uint32_t take(bool want, uint32_t* counter, uint32_t n) {
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t need = __ballot_sync(0xFFFFFFFFu, want);
+        if (!need || exhausted) return UINT32_MAX;
+        const uint32_t k = __popc(need);
+        const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+        const uint32_t have = end - next;
+        uint32_t mine = UINT32_MAX;
+        if (want && rank < have) mine = next + rank;
+        if (k <= have) {
+            next += k;
+        } else {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(counter, 32u);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= n) {
+                exhausted = true;
+                next = end;
+            } else {
+                const uint32_t chunk_end = base + 32u < n ? base + 32u : n;
+                if (want && rank >= have && base + (rank - have) < chunk_end) mine = base + (rank - have);
+                const uint32_t used = k - have;
+                next = base + used < chunk_end ? base + used : chunk_end;
+                end = chunk_end;
+            }
+        }
+        return mine;
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Estimator pieces (src/renderer/renderer.cu:119-262 and helpers)

@@ -42,7 +42,7 @@ struct DevBuf {
 struct crt_scene_s {
     int device = 0;
     crt::Bvh8 bvh;                  // host copy (export / statistics)
-    crt::DevBuf nodes, tris, shade, uvs, mats, light_geo, texels, tex_dims, tex_offsets, error;
+    crt::DevBuf nodes, fnodes, tris, shade, uvs, mats, light_geo, texels, tex_dims, tex_offsets, error;
     crt::DevScene dev{};
     crt_scene_info info{};
     std::vector<uint32_t> lights;   // face indices in pick order
@@ -51,7 +51,7 @@ struct crt_scene_s {
 // Wavefront path-state buffers (see render.cu).
 struct WaveBuffers {
     uint32_t capacity = 0;
-    crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, counters, waves;
+    crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, counters, waves, prof;
 };
 
 namespace crt {

@@ -12,6 +12,7 @@ namespace crt {
 
 int grid_for(uint32_t n, int block, int per_sm);
 int wavefront_pass(crt_render r, uint32_t spp0, uint32_t nspp);
+int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage_profile* out);
 
 constexpr int kMegaBlock = 128;         // 16 x 8 pixel tile, warps of 8 x 4
 constexpr uint32_t kMegaSppPerLaunch = 4;
@@ -19,6 +20,7 @@ constexpr uint32_t kMegaSppPerLaunch = 4;
 // One thread per pixel; samples [spp0, spp0 + nspp) are added to the FP32
 // accumulator in sample order, so the sums equal the reference's per-pass
 // accumulation (`p_imgBuffer[idx] += color`, parallel_renderer.cu:340).
+template <bool F32>
 __global__ void __launch_bounds__(kMegaBlock) mega_kernel(RenderParams P) {
     __shared__ uint2 stack_sh[kStackShared * kMegaBlock];
     Stack st;
@@ -32,7 +34,7 @@ __global__ void __launch_bounds__(kMegaBlock) mega_kernel(RenderParams P) {
         const uint32_t pixel = y * P.width + x;
         float4 acc = P.accum[pixel];
         for (uint32_t s = 0; s < P.nspp; ++s) {
-            const float3 c = sample_path(P, (int)x, (int)y, pixel, P.spp0 + s, st, n_ext, n_shadow);
+            const float3 c = sample_path<F32>(P, (int)x, (int)y, pixel, P.spp0 + s, st, n_ext, n_shadow);
             acc.x = acc.x + c.x;
             acc.y = acc.y + c.y;
             acc.z = acc.z + c.z;
@@ -208,11 +210,26 @@ int crt_render_pass(crt_render r, uint32_t n_spp) {
         dim3 grid((r->width + 15) / 16, (r->height + 7) / 8);
         for (uint32_t done = 0; done < n_spp;) {
             uint32_t k = n_spp - done < kMegaSppPerLaunch ? n_spp - done : kMegaSppPerLaunch;
-            mega_kernel<<<grid, kMegaBlock, 0, r->stream>>>(make_params(r, r->samples_rendered + done, k));
+            if (r->scene->dev.fnodes) mega_kernel<true><<<grid, kMegaBlock, 0, r->stream>>>(make_params(r, r->samples_rendered + done, k));
+            else mega_kernel<false><<<grid, kMegaBlock, 0, r->stream>>>(make_params(r, r->samples_rendered + done, k));
             done += k;
         }
         CRT_CUDA(cudaGetLastError());
     }
+    r->samples_rendered += n_spp;
+    return CRT_OK;
+}
+
+int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out) {
+    if (!r || !out) return set_error(CRT_ERR_INVALID, "null argument");
+    if (r->opts.mode != CRT_MODE_WAVEFRONT)
+        return set_error(CRT_ERR_UNSUPPORTED, "stage profiling needs a wavefront handle");
+    std::memset(out, 0, sizeof(*out));
+    if (n_spp == 0) return CRT_OK;
+    if ((uint64_t)r->samples_rendered + n_spp >= (1ull << 32))
+        return set_error(CRT_ERR_LIMIT, "sample counter overflow");
+    int st = wavefront_profile_pass(r, r->samples_rendered, n_spp, out);
+    if (st != CRT_OK) return st;
     r->samples_rendered += n_spp;
     return CRT_OK;
 }

@@ -144,14 +144,16 @@ CRT_D bool shade_hit(const RenderParams& P, PathState& ps, Ray& ray, const Hit& 
     return true;
 }
 
+template <bool F32>
 CRT_D bool occluded(const DevScene& S, const ShadowReq& sr, Stack& st) {
     Hit h;
     h.t = sr.t_light;
     h.face = (int32_t)sr.light_face;
     h.u = h.v = 0.f;
-    return traverse<true, false>(S, sr.o, sr.d, kEps, h, (int32_t)sr.light_face, st, nullptr);
+    return traverse<true, false, F32>(S, sr.o, sr.d, kEps, h, (int32_t)sr.light_face, st, nullptr);
 }
 
+template <bool F32>
 CRT_D float3 sample_path(const RenderParams& P, int x, int y, uint32_t pixel, uint32_t sample, Stack& st,
                          uint32_t& n_ext, uint32_t& n_shadow) {
     PathState ps;
@@ -163,7 +165,7 @@ CRT_D float3 sample_path(const RenderParams& P, int x, int y, uint32_t pixel, ui
         h.face = -1;
         h.u = h.v = 0.f;
         ++n_ext;
-        traverse<false, false>(P.S, ray.o, ray.d, kEps, h, -1, st, nullptr);
+        traverse<false, false, F32>(P.S, ray.o, ray.d, kEps, h, -1, st, nullptr);
         if (h.face < 0) {
             shade_miss(ps);
             break;
@@ -172,7 +174,7 @@ CRT_D float3 sample_path(const RenderParams& P, int x, int y, uint32_t pixel, ui
         const bool alive = shade_hit(P, ps, ray, h, sr);
         if (sr.valid) {
             ++n_shadow;
-            if (!occluded(P.S, sr, st)) ps.color = ps.color + sr.contrib;
+            if (!occluded<F32>(P.S, sr, st)) ps.color = ps.color + sr.contrib;
         }
         if (!alive) break;
     }

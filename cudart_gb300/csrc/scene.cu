@@ -103,6 +103,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     }
     if (d->num_textures && (!d->texture_dims || !d->texels))
         return set_error(CRT_ERR_INVALID, "textures need dims and texels");
+    if (d->node_format > CRT_NODES_F32) return set_error(CRT_ERR_INVALID, "unknown node format");
 
     auto t0 = std::chrono::steady_clock::now();
     crt_scene s = new crt_scene_s();
@@ -203,6 +204,15 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
         for (uint32_t i = 0; i < dims.back().x; ++i) texels.push_back(f4(0.f, 0.f, 0.f, 0.f));
 
     int st = CRT_OK;
+    const bool f32 = d->node_format == CRT_NODES_F32;
+    if (f32 && !s->bvh.fnodes_ok) {
+        delete s;
+        return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
+    }
+    if (f32 && (st = upload(s->fnodes, s->bvh.fnodes))) {
+        delete s;
+        return st;
+    }
     if ((st = upload(s->nodes, s->bvh.nodes)) || (st = upload(s->tris, s->bvh.tris)) ||
         (st = upload(s->shade, shade)) || (st = upload(s->uvs, uvs)) || (st = upload(s->mats, mats)) ||
         (st = upload(s->light_geo, lgeo)) || (st = upload(s->texels, texels)) ||
@@ -216,6 +226,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
     DevScene& D = s->dev;
     D.nodes = s->nodes.as<float4>();
+    D.fnodes = f32 ? s->fnodes.as<float4>() : nullptr;
     D.tris = s->tris.as<float4>();
     D.shade = s->shade.as<float4>();
     D.uvs = s->uvs.as<float4>();
@@ -237,7 +248,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     I.num_lights = D.n_lights;
     I.num_materials = d->num_materials;
     I.num_textures = d->num_textures;
-    I.node_bytes = s->bvh.nodes.size() * sizeof(Bvh8Node);
+    I.node_bytes = f32 ? s->bvh.fnodes.size() * sizeof(Bvh8FloatNode) : s->bvh.nodes.size() * sizeof(Bvh8Node);
     I.triangle_bytes = s->bvh.tris.size() * sizeof(TriRecord);
     I.shading_bytes = (shade.size() + uvs.size()) * sizeof(float4);
     I.texture_bytes = texels.size() * sizeof(float4);

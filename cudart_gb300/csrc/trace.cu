@@ -10,7 +10,7 @@ namespace crt {
 
 constexpr int kTraceBlock = 128;
 
-template <bool COUNT>
+template <bool COUNT, bool F32>
 __global__ void __launch_bounds__(kTraceBlock) trace_closest_kernel(DevScene S, const float4* __restrict__ rays,
                                                                     uint32_t n, int32_t* __restrict__ out_face,
                                                                     float* __restrict__ out_t,
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_closest_kernel(DevScene S, 
         h.face = -1;
         h.u = h.v = 0.f;
         TraversalStats ts{0, 0};
-        traverse<false, COUNT>(S, xyz(a), xyz(b), a.w, h, -1, st, &ts);
+        traverse<false, COUNT, F32>(S, xyz(a), xyz(b), a.w, h, -1, st, &ts);
         if (COUNT) {
             out_nodes[i] = ts.nodes;
             out_tris[i] = ts.tris;
@@ -65,7 +65,8 @@ int crt_trace_closest(crt_scene s, const float* d_rays, uint32_t n, int32_t* d_i
         return set_error(CRT_ERR_INVALID, "crt_trace_closest: null argument");
     if (n == 0) return CRT_OK;
     if (((uintptr_t)d_rays & 15u) != 0) return set_error(CRT_ERR_INVALID, "rays must be 16-byte aligned");
-    trace_closest_kernel<false><<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
+    auto k = s->dev.fnodes ? trace_closest_kernel<false, true> : trace_closest_kernel<false, false>;
+    k<<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
         s->dev, (const float4*)d_rays, n, d_index, d_t, (float2*)d_uv, nullptr, nullptr);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
@@ -77,7 +78,8 @@ int crt_trace_counts(crt_scene s, const float* d_rays, uint32_t n, uint32_t* d_n
         return set_error(CRT_ERR_INVALID, "crt_trace_counts: null argument");
     if (n == 0) return CRT_OK;
     if (((uintptr_t)d_rays & 15u) != 0) return set_error(CRT_ERR_INVALID, "rays must be 16-byte aligned");
-    trace_closest_kernel<true><<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
+    auto k = s->dev.fnodes ? trace_closest_kernel<true, true> : trace_closest_kernel<true, false>;
+    k<<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
         s->dev, (const float4*)d_rays, n, nullptr, nullptr, nullptr, d_nodes, d_tris);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;

@@ -43,8 +43,12 @@ enum Counter : uint32_t {
     C_FETCH_SHD = 4,    // shadow work counter
     C_CUR = 5,          // which extension queue is current (0/1)
     C_WAVE = 6,         // wave index within the pass
+    C_FETCH_CNT = 7,    // work counter of the profiling count kernels
     C_COUNT = 8
 };
+
+// Profiling totals: extension rays, nodes, triangles; shadow rays, nodes, triangles.
+enum ProfileCounter : uint32_t { P_EXT_RAYS, P_EXT_NODES, P_EXT_TRIS, P_SHD_RAYS, P_SHD_NODES, P_SHD_TRIS, P_COUNT };
 
 struct WaveParams {
     RenderParams R;
@@ -57,6 +61,7 @@ struct WaveParams {
     float4* shadow;     // 3 float4 per request
     uint32_t* counters;
     const uint4* waves; // pixel0, pixel1, sample0, sample1
+    unsigned long long* prof;   // ProfileCounter totals (profiling pass only)
 };
 
 CRT_D uint4 wave_desc(const WaveParams& W) { return W.waves[W.counters[C_WAVE]]; }
@@ -102,35 +107,77 @@ __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
     }
 }
 
+// Persistent work loop shared by the extend and shadow kernels.  REFILL: a
+// lane whose ray finished takes the next queue entry at once (warp-local
+// pool, one global atomic per 32 entries).  Otherwise a warp takes 32 entries
+// and runs all of them to completion before taking more.  Job supplies
+// start(i) (initialise the lane's traversal for queue entry i), step() and
+// finish().
+template <bool REFILL, class Job>
+CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, Job& job) {
+    if (REFILL) {
+        bool active = false;
+        WarpPool pool;
+        pool.init();
+        for (;;) {
+            const uint32_t i = pool.take(!active, fetch, n);
+            if (i != UINT32_MAX) {
+                job.start(i);
+                active = true;
+            }
+            if (!__any_sync(0xFFFFFFFFu, active)) break;
+            if (active && job.step()) {
+                job.finish();
+                active = false;
+            }
+        }
+    } else {
+        const uint32_t lane = threadIdx.x & 31u;
+        for (;;) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(fetch, 32u);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= n) break;
+            if (base + lane < n) {
+                job.start(base + lane);
+                while (!job.step()) {
+                }
+                job.finish();
+            }
+        }
+    }
+}
+
+template <bool WHOLE_LEAF, bool F32>
+struct ExtendJob {
+    const WaveParams& W;
+    const uint32_t* q;
+    Stack& st;
+    Traversal<false, false, WHOLE_LEAF, F32> T;
+    uint32_t path = 0, rays = 0;
+
+    CRT_D ExtendJob(const WaveParams& W_, const uint32_t* q_, Stack& st_) : W(W_), q(q_), st(st_) {}
+    CRT_D void start(uint32_t i) {
+        path = q[i];
+        T.init(xyz(W.st_o[path]), xyz(W.st_d[path]), kEps, FLT_MAX, -1, st);
+    }
+    CRT_D bool step() { return T.step(W.R.S, st, nullptr); }
+    CRT_D void finish() {
+        W.hit[path] = make_float4(T.h.t, __int_as_float(T.h.face), T.h.u, T.h.v);
+        ++rays;
+    }
+};
+
+template <bool REFILL, bool WHOLE_LEAF, bool F32>
 __global__ void __launch_bounds__(kWaveBlock) wf_extend(WaveParams W) {
     __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
     Stack st;
     st.sh = stack_sh + threadIdx.x;
     st.stride = kWaveBlock;
     const uint32_t cur = W.counters[C_CUR];
-    const uint32_t n = W.counters[cur];
-    const uint32_t* q = W.queue[cur];
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t rays = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&W.counters[C_FETCH_EXT], 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        if (i < n) {
-            const uint32_t path = q[i];
-            const float4 o = W.st_o[path], d = W.st_d[path];
-            Hit h;
-            h.t = FLT_MAX;
-            h.face = -1;
-            h.u = h.v = 0.f;
-            traverse<false, false>(W.R.S, xyz(o), xyz(d), kEps, h, -1, st, nullptr);
-            W.hit[path] = make_float4(h.t, __int_as_float(h.face), h.u, h.v);
-            ++rays;
-        }
-    }
-    count_rays(W.R.ray_counts, rays, 0);
+    ExtendJob<WHOLE_LEAF, F32> job(W, W.queue[cur], st);
+    persistent_loop<REFILL>(W.counters[cur], &W.counters[C_FETCH_EXT], job);
+    count_rays(W.R.ray_counts, job.rays, 0);
 }
 
 __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
@@ -184,40 +231,71 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
     }
 }
 
+template <bool WHOLE_LEAF, bool F32>
+struct ShadowJob {
+    const WaveParams& W;
+    Stack& st;
+    Traversal<true, false, WHOLE_LEAF, F32> T;
+    uint32_t entry = 0, rays = 0;
+
+    CRT_D ShadowJob(const WaveParams& W_, Stack& st_) : W(W_), st(st_) {}
+    CRT_D void start(uint32_t i) {
+        entry = i;
+        const float4* e = W.shadow + 3ull * i;
+        const float4 b = e[1];
+        T.init(xyz(e[0]), xyz(b), kEps, b.w, (int32_t)__float_as_uint(e[2].w), st);
+    }
+    CRT_D bool step() { return T.step(W.R.S, st, nullptr); }
+    // a visible light adds the request's contribution to the path colour
+    CRT_D void finish() {
+        ++rays;
+        if (T.occluded) return;
+        const float4* e = W.shadow + 3ull * entry;
+        const uint32_t path = __float_as_uint(e[0].w);
+        const float4 c = e[2];
+        float4 col = W.st_c[path];
+        col.x = col.x + c.x;
+        col.y = col.y + c.y;
+        col.z = col.z + c.z;
+        W.st_c[path] = col;
+    }
+};
+
+template <bool REFILL, bool WHOLE_LEAF, bool F32>
 __global__ void __launch_bounds__(kWaveBlock) wf_shadow(WaveParams W) {
     __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
     Stack st;
     st.sh = stack_sh + threadIdx.x;
     st.stride = kWaveBlock;
-    const uint32_t n = W.counters[C_SHADOW];
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t rays = 0;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&W.counters[C_FETCH_SHD], 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        if (i < n) {
-            const float4* e = W.shadow + 3ull * i;
-            const float4 a = e[0], b = e[1], c = e[2];
-            ShadowReq sr;
-            sr.o = xyz(a);
-            sr.d = xyz(b);
-            sr.t_light = b.w;
-            sr.light_face = __float_as_uint(c.w);
-            ++rays;
-            if (!occluded(W.R.S, sr, st)) {
-                const uint32_t path = __float_as_uint(a.w);
-                float4 col = W.st_c[path];
-                col.x = col.x + c.x;
-                col.y = col.y + c.y;
-                col.z = col.z + c.z;
-                W.st_c[path] = col;
-            }
-        }
-    }
-    count_rays(W.R.ray_counts, 0, rays);
+    ShadowJob<WHOLE_LEAF, F32> job(W, st);
+    persistent_loop<REFILL>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], job);
+    count_rays(W.R.ray_counts, 0, job.rays);
+}
+
+using WaveKernel = void (*)(WaveParams);
+
+// Kernel variants by the CRT_FLAG_* traversal-scheduling flags and the
+// scene's node format.
+template <bool F32>
+static WaveKernel extend_kernel_f(uint32_t flags) {
+    const bool refill = flags & CRT_FLAG_LANE_REFILL, whole = !(flags & CRT_FLAG_SPLIT_LEAF);
+    if (refill) return whole ? wf_extend<true, true, F32> : wf_extend<true, false, F32>;
+    return whole ? wf_extend<false, true, F32> : wf_extend<false, false, F32>;
+}
+
+template <bool F32>
+static WaveKernel shadow_kernel_f(uint32_t flags) {
+    const bool refill = flags & CRT_FLAG_LANE_REFILL, whole = !(flags & CRT_FLAG_SPLIT_LEAF);
+    if (refill) return whole ? wf_shadow<true, true, F32> : wf_shadow<true, false, F32>;
+    return whole ? wf_shadow<false, true, F32> : wf_shadow<false, false, F32>;
+}
+
+static WaveKernel extend_kernel(uint32_t flags, bool f32) {
+    return f32 ? extend_kernel_f<true>(flags) : extend_kernel_f<false>(flags);
+}
+
+static WaveKernel shadow_kernel(uint32_t flags, bool f32) {
+    return f32 ? shadow_kernel_f<true>(flags) : shadow_kernel_f<false>(flags);
 }
 
 __global__ void wf_flip(WaveParams W) {
@@ -245,6 +323,82 @@ __global__ void __launch_bounds__(256) wf_accumulate(WaveParams W) {
 }
 
 __global__ void wf_next_wave(WaveParams W) { W.counters[C_WAVE] += 1; }
+
+__global__ void wf_reset_count_fetch(WaveParams W) { W.counters[C_FETCH_CNT] = 0; }
+
+CRT_D void add_profile(unsigned long long* p, uint32_t rays, uint32_t nodes, uint32_t tris) {
+    const uint32_t r = __reduce_add_sync(0xFFFFFFFFu, rays);
+    const uint32_t n = __reduce_add_sync(0xFFFFFFFFu, nodes);
+    const uint32_t t = __reduce_add_sync(0xFFFFFFFFu, tris);
+    if ((threadIdx.x & 31u) == 0) {
+        atomicAdd(p, (unsigned long long)r);
+        atomicAdd(p + 1, (unsigned long long)n);
+        atomicAdd(p + 2, (unsigned long long)t);
+    }
+}
+
+// Counting re-runs (profiling only): the same traversals as wf_extend /
+// wf_shadow over the same queue entries, tallying node visits and triangle
+// tests instead of writing results.
+template <bool F32>
+__global__ void __launch_bounds__(kWaveBlock) wf_extend_count(WaveParams W) {
+    __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
+    Stack st;
+    st.sh = stack_sh + threadIdx.x;
+    st.stride = kWaveBlock;
+    const uint32_t cur = W.counters[C_CUR];
+    const uint32_t n = W.counters[cur];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t rays = 0;
+    TraversalStats ts{0, 0};
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&W.counters[C_FETCH_CNT], 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            const uint32_t path = W.queue[cur][i];
+            Hit h;
+            h.t = FLT_MAX;
+            h.face = -1;
+            h.u = h.v = 0.f;
+            traverse<false, true, F32>(W.R.S, xyz(W.st_o[path]), xyz(W.st_d[path]), kEps, h, -1, st, &ts);
+            ++rays;
+        }
+    }
+    add_profile(W.prof + P_EXT_RAYS, rays, ts.nodes, ts.tris);
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(kWaveBlock) wf_shadow_count(WaveParams W) {
+    __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
+    Stack st;
+    st.sh = stack_sh + threadIdx.x;
+    st.stride = kWaveBlock;
+    const uint32_t n = W.counters[C_SHADOW];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t rays = 0;
+    TraversalStats ts{0, 0};
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&W.counters[C_FETCH_CNT], 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            const float4* e = W.shadow + 3ull * i;
+            const float4 b = e[1], c = e[2];
+            Hit h;
+            h.t = b.w;
+            h.face = (int32_t)__float_as_uint(c.w);
+            h.u = h.v = 0.f;
+            traverse<true, true, F32>(W.R.S, xyz(e[0]), xyz(b), kEps, h, h.face, st, &ts);
+            ++rays;
+        }
+    }
+    add_profile(W.prof + P_SHD_RAYS, rays, ts.nodes, ts.tris);
+}
 
 int persistent_grid(const void* kernel, int block, size_t smem) {
     int dev = 0, sms = 1, per = 1;
@@ -286,6 +440,7 @@ static int ensure_wave_buffers(crt_render r) {
     CRT_CUDA(B.counters.alloc(C_COUNT * 4));
     CRT_CUDA(cudaMemsetAsync(B.counters.p, 0, C_COUNT * 4, r->stream));
     CRT_CUDA(B.waves.alloc(kMaxWaves * sizeof(uint4)));
+    CRT_CUDA(B.prof.alloc(P_COUNT * sizeof(unsigned long long)));
     destroy_wave_graph(r->wave_graph);   // captured launches hold the old buffers
     r->wave_graph = nullptr;
     return CRT_OK;
@@ -305,77 +460,162 @@ static WaveParams wave_params(crt_render r) {
     W.shadow = B.shadow.as<float4>();
     W.counters = B.counters.as<uint32_t>();
     W.waves = B.waves.as<uint4>();
+    W.prof = B.prof.as<unsigned long long>();
     return W;
 }
 
 struct WaveGrids {
     int gen, ext, shd, acc;
+    WaveKernel extend, shadow, extend_count, shadow_count;
 };
 
-// Grid sizes are queried before a capture starts.
-static WaveGrids wave_grids(uint32_t capacity) {
+// Kernel choice and grid sizes, queried before a capture starts.
+static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32) {
     WaveGrids g;
+    g.extend = extend_kernel(flags, f32);
+    g.shadow = shadow_kernel(flags, f32);
+    g.extend_count = f32 ? wf_extend_count<true> : wf_extend_count<false>;
+    g.shadow_count = f32 ? wf_shadow_count<true> : wf_shadow_count<false>;
     g.gen = grid_for(capacity, kWaveBlock, 16);
-    g.ext = persistent_grid((const void*)wf_extend, kWaveBlock, 0);
-    g.shd = persistent_grid((const void*)wf_shadow, kWaveBlock, 0);
+    g.ext = persistent_grid((const void*)g.extend, kWaveBlock, 0);
+    g.shd = persistent_grid((const void*)g.shadow, kWaveBlock, 0);
     g.acc = grid_for(capacity, 256, 8);
     return g;
 }
 
 // Enqueue one wave; captured into the handle's graph.
 static void enqueue_wave(const WaveParams& W, const WaveGrids& G, uint32_t max_depth, cudaStream_t s) {
-    const int g_gen = G.gen, g_ext = G.ext, g_shd = G.shd;
-    wf_generate<<<g_gen, kWaveBlock, 0, s>>>(W);
+    wf_generate<<<G.gen, kWaveBlock, 0, s>>>(W);
     for (uint32_t b = 0; b < max_depth; ++b) {
-        wf_extend<<<g_ext, kWaveBlock, 0, s>>>(W);
-        wf_shade<<<g_gen, kWaveBlock, 0, s>>>(W);
-        wf_shadow<<<g_shd, kWaveBlock, 0, s>>>(W);
+        G.extend<<<G.ext, kWaveBlock, 0, s>>>(W);
+        wf_shade<<<G.gen, kWaveBlock, 0, s>>>(W);
+        G.shadow<<<G.shd, kWaveBlock, 0, s>>>(W);
         wf_flip<<<1, 1, 0, s>>>(W);
     }
     wf_accumulate<<<G.acc, 256, 0, s>>>(W);
     wf_next_wave<<<1, 1, 0, s>>>(W);
 }
 
-int wavefront_pass(crt_render r, uint32_t spp0, uint32_t nspp) {
-    int st = ensure_wave_buffers(r);
-    if (st != CRT_OK) return st;
-    WaveBuffers& B = r->wave;
-    const uint32_t npix = r->width * r->height;
-    // Wave descriptors: whole sample layers when the image fits, else
-    // pixel ranges of one sample each.
+// Wave descriptors: whole sample layers when the image fits, else pixel
+// ranges of one sample each.
+static std::vector<uint4> make_waves(uint32_t npix, uint32_t capacity, uint32_t spp0, uint32_t nspp) {
     std::vector<uint4> waves;
-    if (npix <= B.capacity) {
-        const uint32_t layers = B.capacity / npix;
+    if (npix <= capacity) {
+        const uint32_t layers = capacity / npix;
         for (uint32_t s = 0; s < nspp; s += layers)
             waves.push_back(make_uint4(0, npix, spp0 + s, spp0 + std::min(nspp, s + layers)));
     } else {
         for (uint32_t s = 0; s < nspp; ++s)
-            for (uint32_t p = 0; p < npix; p += B.capacity)
-                waves.push_back(make_uint4(p, std::min(npix, p + B.capacity), spp0 + s, spp0 + s + 1));
+            for (uint32_t p = 0; p < npix; p += capacity)
+                waves.push_back(make_uint4(p, std::min(npix, p + capacity), spp0 + s, spp0 + s + 1));
     }
+    return waves;
+}
+
+// Uploads one chunk of descriptors and restarts C_CUR / C_WAVE at zero.
+static int upload_waves(crt_render r, const std::vector<uint4>& waves, size_t w0, size_t nw) {
+    WaveBuffers& B = r->wave;
+    const uint32_t zero[2] = {0, 0};
+    CRT_CUDA(cudaMemcpyAsync(B.waves.p, waves.data() + w0, nw * sizeof(uint4), cudaMemcpyHostToDevice,
+                             r->stream));
+    CRT_CUDA(cudaMemcpyAsync(B.counters.as<uint32_t>() + C_CUR, zero, 8, cudaMemcpyHostToDevice, r->stream));
+    return CRT_OK;
+}
+
+int wavefront_pass(crt_render r, uint32_t spp0, uint32_t nspp) {
+    int st = ensure_wave_buffers(r);
+    if (st != CRT_OK) return st;
+    WaveBuffers& B = r->wave;
+    const std::vector<uint4> waves = make_waves(r->width * r->height, B.capacity, spp0, nspp);
     // The wave's launch sequence is captured once per handle and replayed.
     WaveGraph* g = static_cast<WaveGraph*>(r->wave_graph);
     if (!g) {
         g = new WaveGraph();
         r->wave_graph = g;
         const WaveParams W = wave_params(r);
-        const WaveGrids G = wave_grids(B.capacity);
+        const WaveGrids G = wave_grids(B.capacity, r->opts.flags, r->scene->dev.fnodes != nullptr);
         CRT_CUDA(cudaGetLastError());
-        CRT_CUDA(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_wave(W, G, r->opts.max_depth, r->stream);
-        cudaError_t e = cudaStreamEndCapture(r->stream, &g->graph);
+        // Captured on a private stream: the caller's stream may be the legacy
+        // default stream, which cannot be captured.  The graph is launched on
+        // the caller's stream below.
+        cudaStream_t cap = nullptr;
+        CRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_wave(W, G, r->opts.max_depth, cap);
+            e = cudaStreamEndCapture(cap, &g->graph);
+        }
+        cudaStreamDestroy(cap);
         if (e != cudaSuccess) return cuda_error(e, "capture wave graph");
         CRT_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));
     }
-    const uint32_t zero[2] = {0, 0};
     for (size_t w0 = 0; w0 < waves.size(); w0 += kMaxWaves) {
         const size_t nw = std::min<size_t>(kMaxWaves, waves.size() - w0);
-        CRT_CUDA(cudaMemcpyAsync(B.waves.p, waves.data() + w0, nw * sizeof(uint4), cudaMemcpyHostToDevice,
-                                 r->stream));
-        // C_CUR and C_WAVE restart at zero for each chunk of descriptors
-        CRT_CUDA(cudaMemcpyAsync(B.counters.as<uint32_t>() + C_CUR, zero, 8, cudaMemcpyHostToDevice, r->stream));
+        if ((st = upload_waves(r, waves, w0, nw)) != CRT_OK) return st;
         for (size_t w = 0; w < nw; ++w) CRT_CUDA(cudaGraphLaunch(g->exec, r->stream));
     }
+    return CRT_OK;
+}
+
+// Same launch sequence as enqueue_wave(), one kernel at a time with CUDA
+// events around each launch, plus untimed counting re-runs of each traversal.
+int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage_profile* out) {
+    int st = ensure_wave_buffers(r);
+    if (st != CRT_OK) return st;
+    WaveBuffers& B = r->wave;
+    const std::vector<uint4> waves = make_waves(r->width * r->height, B.capacity, spp0, nspp);
+    const WaveParams W = wave_params(r);
+    const WaveGrids G = wave_grids(B.capacity, r->opts.flags, r->scene->dev.fnodes != nullptr);
+    CRT_CUDA(cudaMemsetAsync(B.prof.p, 0, B.prof.bytes, r->stream));
+    cudaEvent_t e0, e1;
+    CRT_CUDA(cudaEventCreate(&e0));
+    CRT_CUDA(cudaEventCreate(&e1));
+    cudaStream_t s = r->stream;
+    cudaError_t err = cudaSuccess;
+    auto timed = [&](int stage, auto launch) {
+        if (err != cudaSuccess) return;
+        cudaEventRecord(e0, s);
+        launch();
+        cudaEventRecord(e1, s);
+        err = cudaEventSynchronize(e1);
+        if (err == cudaSuccess) err = cudaGetLastError();
+        float ms = 0.f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        out->ms[stage] += ms;
+        out->launches[stage] += 1;
+    };
+    for (size_t w0 = 0; w0 < waves.size() && err == cudaSuccess; w0 += kMaxWaves) {
+        const size_t nw = std::min<size_t>(kMaxWaves, waves.size() - w0);
+        if ((st = upload_waves(r, waves, w0, nw)) != CRT_OK) break;
+        for (size_t w = 0; w < nw; ++w) {
+            timed(0, [&] { wf_generate<<<G.gen, kWaveBlock, 0, s>>>(W); });
+            for (uint32_t b = 0; b < r->opts.max_depth; ++b) {
+                timed(1, [&] { G.extend<<<G.ext, kWaveBlock, 0, s>>>(W); });
+                wf_reset_count_fetch<<<1, 1, 0, s>>>(W);
+                G.extend_count<<<G.ext, kWaveBlock, 0, s>>>(W);
+                timed(2, [&] { wf_shade<<<G.gen, kWaveBlock, 0, s>>>(W); });
+                timed(3, [&] { G.shadow<<<G.shd, kWaveBlock, 0, s>>>(W); });
+                wf_reset_count_fetch<<<1, 1, 0, s>>>(W);
+                G.shadow_count<<<G.shd, kWaveBlock, 0, s>>>(W);
+                timed(5, [&] { wf_flip<<<1, 1, 0, s>>>(W); });
+            }
+            timed(4, [&] { wf_accumulate<<<G.acc, 256, 0, s>>>(W); });
+            timed(5, [&] { wf_next_wave<<<1, 1, 0, s>>>(W); });
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != CRT_OK) return st;
+    if (err != cudaSuccess) return cuda_error(err, "profiled wavefront pass");
+    unsigned long long c[P_COUNT];
+    CRT_CUDA(cudaMemcpyAsync(c, B.prof.p, sizeof(c), cudaMemcpyDeviceToHost, s));
+    CRT_CUDA(cudaStreamSynchronize(s));
+    out->extension_rays += c[P_EXT_RAYS];
+    out->extension_nodes += c[P_EXT_NODES];
+    out->extension_tris += c[P_EXT_TRIS];
+    out->shadow_rays += c[P_SHD_RAYS];
+    out->shadow_nodes += c[P_SHD_NODES];
+    out->shadow_tris += c[P_SHD_TRIS];
     return CRT_OK;
 }
 

@@ -56,7 +56,8 @@ def bvh_build_host(positions: np.ndarray):
 class GB300Scene:
     """Scene handle: BVH, triangles, materials, lights and textures on the GPU."""
 
-    def __init__(self, sc: SceneArrays, lights: Optional[np.ndarray] = None):
+    def __init__(self, sc: SceneArrays, lights: Optional[np.ndarray] = None,
+                 node_format: str = "q8"):
         L = load()
         self.arrays = sc
         self._keep = []
@@ -83,7 +84,8 @@ class GB300Scene:
                          len(lights) if lights is not None else 0,
                          li.ctypes.data if lights is not None else None,
                          len(sc.textures), dims.ctypes.data if len(dims) else None,
-                         texels.ctypes.data)
+                         texels.ctypes.data, {"q8": _lib.NODES_Q8, "f32": _lib.NODES_F32}[node_format])
+        self.node_format = node_format
         h = C.c_void_p()
         check(L.crt_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
@@ -137,7 +139,8 @@ class GB300Renderer:
 
     def __init__(self, scene: GB300Scene, width: int, height: int, samples: int,
                  camera: Optional[Camera] = None, max_depth: int = 6, seed: int = 1234,
-                 mode: str = "megakernel", view_id: int = 0, wave_paths: int = 0):
+                 mode: str = "megakernel", view_id: int = 0, wave_paths: int = 0,
+                 flags: int = 0):
         L = load()
         self.scene = scene
         self.width, self.height, self.samples = width, height, samples
@@ -151,6 +154,7 @@ class GB300Renderer:
         opts.view_id = view_id
         opts.mode = {"megakernel": _lib.MODE_MEGAKERNEL, "wavefront": _lib.MODE_WAVEFRONT}[mode]
         opts.wave_paths = wave_paths
+        opts.flags = flags
         h = C.c_void_p()
         check(L.crt_render_create(scene.handle, C.byref(camera), width, height, C.byref(opts),
                                   C.byref(h)))
@@ -210,6 +214,17 @@ class GB300Renderer:
 
     def set_stream(self, stream: int) -> None:
         check(load().crt_render_set_stream(self.handle, stream))
+
+    def profile_pass(self, n_spp: int) -> dict:
+        """Wavefront pass with per-stage CUDA-event timing and traversal counts."""
+        p = _lib.StageProfile()
+        check(load().crt_render_profile_pass(self.handle, n_spp, C.byref(p)))
+        out = {f"{s}_ms": p.ms[i] for i, s in enumerate(p.STAGES)}
+        out.update({f"{s}_launches": p.launches[i] for i, s in enumerate(p.STAGES)})
+        for f in ("extension_rays", "extension_nodes", "extension_tris", "shadow_rays",
+                  "shadow_nodes", "shadow_tris"):
+            out[f] = getattr(p, f)
+        return out
 
     def ray_counts(self):
         e, s = C.c_uint64(0), C.c_uint64(0)

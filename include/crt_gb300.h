@@ -107,7 +107,16 @@ typedef struct {
     const uint32_t* texture_dims;  /* [num_textures][width, height] */
     const float* texels;           /* [sum(w*h)][rgb] linear floats, as
                                       stbi_loadf returns them */
+    uint32_t node_format;          /* crt_node_format */
 } crt_scene_desc;
+
+/* BVH node encoding on the device (same tree either way). */
+typedef enum {
+    CRT_NODES_Q8 = 0,    /* 80-byte nodes, child planes quantised to 8 bits
+                            relative to the node and rounded outward */
+    CRT_NODES_F32 = 1    /* 208-byte nodes with FP32 child planes: more bytes
+                            per visit, half the ALU work per child test */
+} crt_node_format;
 
 typedef struct crt_scene_s* crt_scene;
 typedef struct crt_render_s* crt_render;
@@ -181,6 +190,16 @@ typedef enum {
     CRT_MODE_WAVEFRONT = 1     /* generate / extend / shade / shadow queues */
 } crt_mode;
 
+/* Traversal scheduling of the wavefront's persistent kernels.  The default
+ * (0): a warp takes 32 rays and finishes them all before taking more, and a
+ * node visit tests all triangles of the leaves it hits. */
+enum {
+    CRT_FLAG_LANE_REFILL = 1u,  /* a lane whose ray finished takes the next one
+                                   at once (warp-local pool of queue entries) */
+    CRT_FLAG_SPLIT_LEAF = 2u    /* one triangle test per traversal step, so lanes
+                                   in leaves and lanes in inner nodes interleave */
+};
+
 typedef struct {
     uint32_t max_depth;        /* bounces per path; the reference hard-codes 6
                                   (renderer.cu:25,33) */
@@ -189,6 +208,7 @@ typedef struct {
     uint32_t mode;             /* crt_mode */
     uint32_t block_size;       /* 0 = library default */
     uint32_t wave_paths;       /* wavefront: paths in flight, 0 = default */
+    uint32_t flags;            /* CRT_FLAG_* */
 } crt_render_options;
 
 CRT_EXPORT void crt_render_options_default(crt_render_options* opts);
@@ -215,6 +235,20 @@ CRT_EXPORT int crt_render_reset(crt_render r);
 CRT_EXPORT int crt_render_set_camera(crt_render r, const crt_camera* camera);
 /* Use the caller's CUDA stream (cudaStream_t) instead of the handle's own. */
 CRT_EXPORT int crt_render_set_stream(crt_render r, void* stream);
+/* Per-stage timing of a wavefront pass, for the memory roofline. */
+typedef struct {
+    double ms[6];              /* generate, extend, shade, shadow, accumulate, bookkeeping */
+    uint64_t launches[6];
+    uint64_t extension_rays, extension_nodes, extension_tris;
+    uint64_t shadow_rays, shadow_nodes, shadow_tris;
+} crt_stage_profile;
+
+/* Renders n_spp more samples per pixel (like crt_render_pass, same result)
+ * with the wavefront stages launched one by one instead of through the
+ * graph, each timed with CUDA events on the handle's stream; every
+ * extension and shadow traversal is re-run untimed in counting mode to
+ * report node visits and triangle tests.  Wavefront handles only. */
+CRT_EXPORT int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out);
 /* Extension and shadow rays traced by the passes since the last reset. */
 CRT_EXPORT int crt_render_ray_counts(crt_render r, uint64_t* extension_rays, uint64_t* shadow_rays);
 

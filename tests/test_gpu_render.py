@@ -43,6 +43,27 @@ def test_wavefront_equals_megakernel(cuda):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("flags", [1, 2, 3])
+def test_scheduling_flags_do_not_change_results(cuda, flags):
+    sc = scenes.cornell_box(width=96, height=64)
+    a = _render(sc, 8, 5, "wavefront", wave_paths=1 << 15).accum()
+    b = _render(sc, 8, 5, "wavefront", wave_paths=1 << 15, flags=flags).accum()
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("mode", ["megakernel", "wavefront"])
+def test_f32_nodes_render_identically(cuda, mode):
+    sc = scenes.large_textured(width=96, height=54, grid=64, tex_size=64, n_spheres=12,
+                               sphere_subdiv=2)
+    out = []
+    for fmt in ("q8", "f32"):
+        g = GB300Scene(sc, node_format=fmt)
+        r = GB300Renderer(g, sc.width, sc.height, 8, max_depth=8, mode=mode)
+        r.render()
+        out.append(r.accum())
+    assert np.array_equal(out[0], out[1])
+
+
 def test_progressive_passes_equal_single(cuda):
     sc = scenes.cornell_box(width=64, height=64)
     g = GB300Scene(sc)

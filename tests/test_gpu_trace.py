@@ -11,8 +11,8 @@ from cudart_gb300 import GB300Scene, scenes
 pytestmark = pytest.mark.gpu
 
 
-def _check(cuda, sc, rays, brute=True):
-    g = GB300Scene(sc)
+def _check(cuda, sc, rays, brute=True, node_format="q8"):
+    g = GB300Scene(sc, node_format=node_format)
     idx, t, uv = g.trace_closest(cuda.from_numpy(rays).cuda())
     o = oracle.OracleScene(sc)
     oi, ot, ouv = o.closest_hit(rays, brute=brute)
@@ -48,14 +48,24 @@ def test_cornell_ties_lowest_index(cuda):
     assert np.any((oi >= floor[2]) & (oi < floor[2] + floor[3]))
 
 
-def test_mixed_scene_bvh_oracle(cuda):
+@pytest.mark.parametrize("fmt", ["q8", "f32"])
+def test_mixed_scene_bvh_oracle(cuda, fmt):
     sc = scenes.mixed_mid(subdiv=3)
-    _check(cuda, sc, random_rays(20000, 2))
+    _check(cuda, sc, random_rays(20000, 2), node_format=fmt)
 
 
-def test_textured_scene(cuda):
+@pytest.mark.parametrize("fmt", ["q8", "f32"])
+def test_textured_scene(cuda, fmt):
     sc = scenes.large_textured(grid=64, tex_size=64, n_spheres=8, sphere_subdiv=2)
-    _check(cuda, sc, random_rays(20000, 4, lo=-4.0, hi=4.0))
+    _check(cuda, sc, random_rays(20000, 4, lo=-4.0, hi=4.0), node_format=fmt)
+
+
+def test_f32_nodes_cornell_ties_and_windows(cuda):
+    sc = scenes.cornell_box()
+    rays = random_rays(6000, 8)
+    rays[2000:4000, 3] = 0.3
+    rays[4000:, 7] = 0.7
+    _check(cuda, sc, rays, node_format="f32")
 
 
 def test_axis_parallel_and_windows(cuda):
