@@ -106,7 +106,10 @@ SIGNATURES = {
     "crt_render_set_stream": (C.c_int, [P, P]),
     "crt_render_ray_counts": (C.c_int, [P, P, P]),
     "crt_render_profile_pass": (C.c_int, [P, U32, P]),
+    "crt_render_tile_noalloc": (C.c_int, [P, P, U32, U32, P, U32, U32, U32, U32, P, P]),
 }
+
+NOALLOC_MAX_PATHS = 65536
 
 _lib = None
 

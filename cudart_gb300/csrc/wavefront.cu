@@ -24,6 +24,7 @@
 #include "render_common.cuh"
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 namespace crt {
@@ -621,4 +622,129 @@ int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage
 
 void destroy_wave_graph(void* g) { delete static_cast<WaveGraph*>(g); }
 
+// ---------------------------------------------------------------------------
+// Allocation-free tile renders (crt_render_tile_noalloc).
+//
+// Some callers cannot allocate device memory at render time: a host
+// application that owns every device allocation through its own pool (a
+// plugin inside a DCC tool or game engine), or a latency-sensitive loop that
+// must not pay for cudaMalloc / cudaFree and the synchronisation they imply.
+// For them the wavefront kernels can run on a fixed scratch area that lives
+// in this file as a static device array: every GPU that loads the library
+// holds kNoAllocBytes (about 8.5 MiB) of it until the process exits.  The
+// caller brings the inputs (a scene) and the output (an accumulator); the
+// paths in flight, queues, counters and the wave descriptor use the scratch.
+// ---------------------------------------------------------------------------
+Camera to_device_camera(const crt_camera& c);
+
+constexpr uint32_t kNoAllocPaths = CRT_NOALLOC_MAX_PATHS;
+constexpr size_t kNoAllocOff[] = {
+    0,                                  // ray_o    16 B per path
+    16ull * kNoAllocPaths,              // ray_d
+    32ull * kNoAllocPaths,              // color
+    48ull * kNoAllocPaths,              // mask
+    64ull * kNoAllocPaths,              // hit
+    80ull * kNoAllocPaths,              // queue 0  4 B per path
+    84ull * kNoAllocPaths,              // queue 1
+    88ull * kNoAllocPaths,              // shadow requests 48 B per path
+    136ull * kNoAllocPaths,             // counters (C_COUNT words), then the wave descriptor
+    136ull * kNoAllocPaths + 256,       // ray counts (2 x u64)
+};
+constexpr size_t kNoAllocBytes = 136ull * kNoAllocPaths + 512;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the scratch on each device, looked up once per device.
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_addr[64] = {};
+
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    CRT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(CRT_ERR_LIMIT, "device ordinal above 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        // the array's host-side name is only a handle: the kernels need the
+        // device address, which belongs to the current device
+        CRT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return CRT_OK;
+}
+
+// Starts a call: clears the counters and ray counts and installs the wave
+// descriptor (everything that must start at zero; path state is always
+// written before it is read).
+__global__ void wf_noalloc_begin(WaveParams W, uint4 wave) {
+    for (int i = 0; i < C_COUNT; ++i) W.counters[i] = 0;
+    W.R.ray_counts[0] = W.R.ray_counts[1] = 0;
+    const_cast<uint4*>(W.waves)[0] = wave;
+}
+
 }  // namespace crt
+
+using namespace crt;
+
+extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera, uint32_t width,
+                                       uint32_t height, const crt_render_options* opts, uint32_t pixel0,
+                                       uint32_t pixel_count, uint32_t spp0, uint32_t nspp, float* d_accum,
+                                       void* stream) {
+    if (!scene || !camera || !d_accum) return set_error(CRT_ERR_INVALID, "crt_render_tile_noalloc: null argument");
+    if (width == 0 || height == 0 || (uint64_t)width * height >= (1ull << 31))
+        return set_error(CRT_ERR_INVALID, "crt_render_tile_noalloc: bad image size");
+    if (pixel_count == 0 || nspp == 0) return CRT_OK;
+    if ((uint64_t)pixel0 + pixel_count > (uint64_t)width * height)
+        return set_error(CRT_ERR_INVALID, "crt_render_tile_noalloc: pixel range outside the image");
+    if ((uint64_t)pixel_count * nspp > kNoAllocPaths)
+        return set_error(CRT_ERR_LIMIT, "crt_render_tile_noalloc: pixel_count * nspp exceeds "
+                                        "CRT_NOALLOC_MAX_PATHS (65536 paths in flight)");
+    if ((uint64_t)spp0 + nspp >= (1ull << 32)) return set_error(CRT_ERR_LIMIT, "sample index overflow");
+    if (((uintptr_t)d_accum & 15u) != 0) return set_error(CRT_ERR_INVALID, "d_accum must be 16-byte aligned");
+    crt_render_options o;
+    if (opts) o = *opts;
+    else crt_render_options_default(&o);
+    if (o.max_depth == 0 || o.max_depth > 1024) return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
+    void* base = nullptr;
+    int st = noalloc_scratch(&base);
+    if (st != CRT_OK) return st;
+    unsigned char* b = static_cast<unsigned char*>(base);
+    WaveParams W;
+    RenderParams& R = W.R;
+    R.S = scene->dev;
+    R.cam = to_device_camera(*camera);
+    R.accum = reinterpret_cast<float4*>(d_accum);
+    R.width = width;
+    R.height = height;
+    R.seed = o.seed;
+    R.view = o.view_id;
+    R.spp0 = spp0;
+    R.nspp = nspp;
+    R.max_depth = o.max_depth;
+    R.ray_counts = reinterpret_cast<unsigned long long*>(b + kNoAllocOff[9]);
+    W.st_o = reinterpret_cast<float4*>(b + kNoAllocOff[0]);
+    W.st_d = reinterpret_cast<float4*>(b + kNoAllocOff[1]);
+    W.st_c = reinterpret_cast<float4*>(b + kNoAllocOff[2]);
+    W.st_m = reinterpret_cast<float4*>(b + kNoAllocOff[3]);
+    W.hit = reinterpret_cast<float4*>(b + kNoAllocOff[4]);
+    W.queue[0] = reinterpret_cast<uint32_t*>(b + kNoAllocOff[5]);
+    W.queue[1] = reinterpret_cast<uint32_t*>(b + kNoAllocOff[6]);
+    W.shadow = reinterpret_cast<float4*>(b + kNoAllocOff[7]);
+    W.counters = reinterpret_cast<uint32_t*>(b + kNoAllocOff[8]);
+    W.waves = reinterpret_cast<const uint4*>(b + kNoAllocOff[8] + 64);
+    W.prof = nullptr;
+    const WaveGrids G = wave_grids(kNoAllocPaths, o.flags, scene->dev.fnodes != nullptr);
+    cudaStream_t s = (cudaStream_t)stream;
+    wf_noalloc_begin<<<1, 1, 0, s>>>(W, make_uint4(pixel0, pixel0 + pixel_count, spp0, spp0 + nspp));
+    wf_generate<<<G.gen, kWaveBlock, 0, s>>>(W);
+    for (uint32_t k = 0; k < o.max_depth; ++k) {
+        G.extend<<<G.ext, kWaveBlock, 0, s>>>(W);
+        wf_shade<<<G.gen, kWaveBlock, 0, s>>>(W);
+        G.shadow<<<G.shd, kWaveBlock, 0, s>>>(W);
+        wf_flip<<<1, 1, 0, s>>>(W);
+    }
+    wf_accumulate<<<G.acc, 256, 0, s>>>(W);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}

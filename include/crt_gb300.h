@@ -249,6 +249,36 @@ typedef struct {
  * extension and shadow traversal is re-run untimed in counting mode to
  * report node visits and triangle tests.  Wavefront handles only. */
 CRT_EXPORT int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out);
+/* ---- allocation-free tile render ----------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory while rendering, such as a host application that
+ * owns every device allocation through its own pool (a plugin inside a DCC
+ * tool or engine), or a latency-critical loop that must not pay for
+ * cudaMalloc / cudaFree and the device synchronisation they cause.
+ *
+ * Renders samples [spp0, spp0 + nspp) of the pixels [pixel0, pixel0 +
+ * pixel_count) of a width x height image with the wavefront kernels and
+ * adds each pixel's per-sample radiance, in sample order, to d_accum[pixel]
+ * (the caller's device buffer of width*height x 4 floats: rgb + unused,
+ * 16-byte aligned; same layout as crt_render_accum_device).  Sums are
+ * bit-identical to crt_render_pass when calls cover each pixel's samples in
+ * increasing order.  Asynchronous on `stream` (NULL = legacy default).
+ *
+ * The call allocates nothing: paths in flight, queues and counters live in
+ * a fixed scratch array compiled into the library (about 8.5 MiB of device
+ * memory on every GPU that loads it, held until the process exits).  Hence
+ * pixel_count * nspp may not exceed CRT_NOALLOC_MAX_PATHS; larger requests
+ * fail with CRT_ERR_LIMIT, so render big images as several tiles.  The
+ * first call on a device looks up the scratch array's device address; make
+ * that first call before any stream capture.  All calls share the one
+ * scratch array, so calls that can overlap on the GPU (different streams,
+ * or different threads without ordering) race: serialise them. */
+#define CRT_NOALLOC_MAX_PATHS 65536u
+CRT_EXPORT int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera, uint32_t width,
+                                       uint32_t height, const crt_render_options* opts,
+                                       uint32_t pixel0, uint32_t pixel_count, uint32_t spp0,
+                                       uint32_t nspp, float* d_accum, void* stream);
+
 /* Extension and shadow rays traced by the passes since the last reset. */
 CRT_EXPORT int crt_render_ray_counts(crt_render r, uint64_t* extension_rays, uint64_t* shadow_rays);
 
