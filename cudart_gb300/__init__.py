@@ -5,8 +5,9 @@ include/crt_gb300.h); this package is its host-side mirror of the
 reference's renderer interface plus the seeded synthetic workloads.
 """
 from ._lib import CrtError, load
-from .renderer import GB300Renderer, GB300Scene, bvh_build_host, camera_from_json
+from .renderer import (GB300Batch, GB300Renderer, GB300Scene, autotune, bvh_build_host,
+                       camera_from_json, make_options, options_dict)
 from . import scenes
 
-__all__ = ["CrtError", "GB300Renderer", "GB300Scene", "bvh_build_host", "camera_from_json",
-           "load", "scenes"]
+__all__ = ["CrtError", "GB300Batch", "GB300Renderer", "GB300Scene", "autotune", "bvh_build_host",
+           "camera_from_json", "load", "make_options", "options_dict", "scenes"]

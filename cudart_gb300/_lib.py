@@ -39,13 +39,21 @@ class Camera(C.Structure):
                 ("ypixels", C.c_int32)]
 
 
+class View(C.Structure):
+    _fields_ = [("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("spp", C.c_uint32), ("view_id", C.c_uint32)]
+
+
+MAX_VIEWS = 8192
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("num_triangles", C.c_uint32), ("positions", C.c_void_p),
                 ("normals", C.c_void_p), ("uvs", C.c_void_p), ("material_ids", C.c_void_p),
                 ("num_materials", C.c_uint32), ("materials", C.c_void_p),
                 ("num_lights", C.c_uint32), ("light_indices", C.c_void_p),
                 ("num_textures", C.c_uint32), ("texture_dims", C.c_void_p),
-                ("texels", C.c_void_p), ("node_format", C.c_uint32)]
+                ("texels", C.c_void_p), ("node_format", C.c_uint32), ("bvh_width", C.c_uint32)]
 
 
 NODES_Q8 = 0
@@ -58,7 +66,7 @@ class SceneInfo(C.Structure):
                 ("num_materials", C.c_uint32), ("num_textures", C.c_uint32),
                 ("node_bytes", C.c_uint64), ("triangle_bytes", C.c_uint64),
                 ("shading_bytes", C.c_uint64), ("texture_bytes", C.c_uint64),
-                ("lights_area", C.c_float), ("build_ms", C.c_float)]
+                ("lights_area", C.c_float), ("build_ms", C.c_float), ("bvh_width", C.c_uint32)]
 
 
 class StageProfile(C.Structure):
@@ -66,13 +74,26 @@ class StageProfile(C.Structure):
     _fields_ = [("ms", C.c_double * 6), ("launches", C.c_uint64 * 6),
                 ("extension_rays", C.c_uint64), ("extension_nodes", C.c_uint64),
                 ("extension_tris", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("shadow_nodes", C.c_uint64), ("shadow_tris", C.c_uint64)]
+                ("shadow_nodes", C.c_uint64), ("shadow_tris", C.c_uint64),
+                ("extend_ms_by_bounce", C.c_double * 16), ("extend_rays_by_bounce", C.c_uint64 * 16),
+                ("shadow_ms_by_bounce", C.c_double * 16), ("shadow_rays_by_bounce", C.c_uint64 * 16)]
 
 
 class RenderOptions(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("seed", C.c_uint64), ("view_id", C.c_uint32),
                 ("mode", C.c_uint32), ("block_size", C.c_uint32), ("wave_paths", C.c_uint32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("wave_sets", C.c_uint32), ("stack_depth", C.c_uint32),
+                ("node_format", C.c_int32), ("queue_chunk", C.c_uint32)]
+
+
+class TuneParams(C.Structure):
+    _fields_ = [("trial_spp", C.c_uint32), ("repeats", C.c_uint32), ("rounds", C.c_uint32),
+                ("tune_bvh_width", C.c_uint32), ("max_wave_bytes", C.c_uint64)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("options", RenderOptions), ("bvh_width", C.c_uint32), ("candidates", C.c_uint32),
+                ("ms_per_spp", C.c_float), ("start_ms_per_spp", C.c_float), ("tune_ms", C.c_float)]
 
 
 FLAG_LANE_REFILL = 1
@@ -89,7 +110,8 @@ SIGNATURES = {
     "crt_scene_destroy": (C.c_int, [P]),
     "crt_scene_get_info": (C.c_int, [P, P]),
     "crt_scene_export_bvh": (C.c_int, [P, P, P]),
-    "crt_bvh_build_host": (C.c_int, [P, U32, P, P, P, P]),
+    "crt_bvh_build_host": (C.c_int, [P, U32, U32, P, P, P, P]),
+    "crt_scene_set_bvh_width": (C.c_int, [P, U32]),
     "crt_trace_closest": (C.c_int, [P, P, U32, P, P, P, P]),
     "crt_trace_counts": (C.c_int, [P, P, U32, P, P, P]),
     "crt_render_options_default": (None, [P]),
@@ -105,8 +127,16 @@ SIGNATURES = {
     "crt_render_set_camera": (C.c_int, [P, P]),
     "crt_render_set_stream": (C.c_int, [P, P]),
     "crt_render_ray_counts": (C.c_int, [P, P, P]),
+    "crt_tune_params_default": (None, [P]),
+    "crt_autotune": (C.c_int, [P, P, U32, U32, P, P, P]),
     "crt_render_profile_pass": (C.c_int, [P, U32, P]),
     "crt_render_tile_noalloc": (C.c_int, [P, P, U32, U32, P, U32, U32, U32, U32, P, P]),
+    "crt_batch_create": (C.c_int, [P, P, U32, P, P]),
+    "crt_render_adjoint": (C.c_int, [P, U32, U32, P, P, P]),
+    "crt_batch_render": (C.c_int, [P]),
+    "crt_render_view_info": (C.c_int, [P, U32, P, P, P]),
+    "crt_render_view_resolve": (C.c_int, [P, U32, P]),
+    "crt_render_view_accum": (C.c_int, [P, U32, P]),
 }
 
 NOALLOC_MAX_PATHS = 65536

@@ -157,7 +157,8 @@ int scale_exponent(double ext) {
 }  // namespace
 
 bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
-                uint32_t max_levels, Bvh8& out, const char** msg) {
+                uint32_t max_levels, Bvh8& out, const char** msg, int max_children) {
+    if (max_children != 4 && max_children != 8) { *msg = "BVH width must be 4 or 8"; return false; }
     if (n == 0) { *msg = "scene has no triangles"; return false; }
     // Margin: 2^-15 of the largest coordinate magnitude (at least 2^-15).
     double scale = 1.0;
@@ -215,7 +216,7 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
         } else {
             ch[nch++] = n2[it.n2].left;
             ch[nch++] = n2[it.n2].right;
-            while (nch < 8) {
+            while (nch < max_children) {
                 int best = -1;
                 float area = -1.f;
                 for (int c = 0; c < nch; ++c)

@@ -68,7 +68,8 @@ struct Bvh8 {
 // v1/e1/e2: [n][3] floats as the scene computes them (e = v - v1, in FP32).
 // Returns false (with msg) if the scene is empty or the tree exceeds
 // max_levels levels.
+// max_children: 8, or 4 for a narrower tree stored in the same node layout.
 bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
-                uint32_t max_levels, Bvh8& out, const char** msg);
+                uint32_t max_levels, Bvh8& out, const char** msg, int max_children = 8);
 
 }  // namespace crt

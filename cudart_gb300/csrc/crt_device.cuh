@@ -22,11 +22,13 @@ constexpr int kNoTexture = -1;
 
 enum Bsdf : int { DIFFUSE = 0, SPECULAR = 1, DIFFSPEC = 2, MICROFACET = 3, REFRACTIVE = 4, EMISSIVE = 5 };
 
-// Traversal stack: kStackShared entries per thread in shared memory, then
-// kStackLocal more in local memory (touched only by very deep trees).
+// Traversal stack: the first entries of each thread's stack live in shared
+// memory (kStackShared by default, or the launch's chosen depth, at most
+// kStackSharedMax), the rest in local memory, which only very deep trees
+// touch.  A traversal never holds more than kMaxLevels entries.
 constexpr int kStackShared = 16;
-constexpr int kStackLocal = 48;
-constexpr int kMaxLevels = kStackShared + kStackLocal;
+constexpr int kStackSharedMax = 32;
+constexpr int kMaxLevels = 64;
 constexpr uint32_t kMaxNodeVisits = 1u << 20;   // watchdog per traversal
 
 enum ErrorBits : uint32_t { ERR_WATCHDOG = 1u, ERR_STACK = 2u };
@@ -163,19 +165,26 @@ struct TraversalStats {
 // Per-thread stack: shared-memory part (stride = threads per block) and a
 // local-memory overflow part.
 struct Stack {
-    uint2* sh;
-    uint32_t stride;
+    uint2* sh;           // this thread's first shared entry; entries are `stride` apart
+    uint32_t stride;     // threads per block
+    int depth;           // entries kept in shared memory
     int sp;
-    uint2 spill[kStackLocal];
+    uint2 spill[kMaxLevels];
 
+    CRT_D void setup(uint2* base, uint32_t threads, int shared_depth) {
+        sh = base + threadIdx.x;
+        stride = threads;
+        depth = shared_depth;
+        sp = 0;
+    }
     CRT_D void push(uint2 e) {
-        if (sp < kStackShared) sh[sp * stride] = e;
-        else spill[sp - kStackShared] = e;
+        if (sp < depth) sh[sp * stride] = e;
+        else spill[sp - depth] = e;
         ++sp;
     }
     CRT_D uint2 pop() {
         --sp;
-        return sp < kStackShared ? sh[sp * stride] : spill[sp - kStackShared];
+        return sp < depth ? sh[sp * stride] : spill[sp - depth];
     }
 };
 
@@ -638,13 +647,17 @@ CRT_D float3 light_point(const LightGeo& l, float pu, float pv) {
 
 // Contribution of estimateDirectLighting after a successful shadow test
 // (src/renderer/renderer.cu:436-443): ka_light * A |cos| / (d^2 A_total).
-CRT_D float3 light_contribution(const DevScene& S, const LightGeo& l, float3 lcolor, float t,
-                                float lu, float lv, float3 dir) {
+// Geometry weight of a light sample: the contribution is lcolor * weight.
+CRT_D float light_weight(const DevScene& S, const LightGeo& l, float t, float lu, float lv, float3 dir) {
     const Shading ls = load_shading(S, l.face);
     const float d2 = t * t;
     const float cost = fabsf(dot(shading_normal(ls, lu, lv), dir * -1.0f));
-    const float wgt = l.area / (d2 * S.lights_area) * cost;
-    return f3(0.f, 0.f, 0.f) + lcolor * wgt;
+    return l.area / (d2 * S.lights_area) * cost;
+}
+
+CRT_D float3 light_contribution(const DevScene& S, const LightGeo& l, float3 lcolor, float t,
+                                float lu, float lv, float3 dir) {
+    return f3(0.f, 0.f, 0.f) + lcolor * light_weight(S, l, t, lu, lv, dir);
 }
 
 }  // namespace crt

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/crt_gb300.h"
@@ -35,6 +36,10 @@ struct DevBuf {
         return n ? cudaMalloc(&p, n) : cudaSuccess;
     }
     template <typename T> T* as() const { return static_cast<T*>(p); }
+    void swap(DevBuf& o) {
+        std::swap(p, o.p);
+        std::swap(bytes, o.bytes);
+    }
 };
 
 }  // namespace crt
@@ -43,31 +48,103 @@ struct crt_scene_s {
     int device = 0;
     crt::Bvh8 bvh;                  // host copy (export / statistics)
     crt::DevBuf nodes, fnodes, tris, shade, uvs, mats, light_geo, texels, tex_dims, tex_offsets, error;
-    crt::DevScene dev{};
+    crt::DevScene dev{};            // both node encodings uploaded
+    bool default_f32 = false;       // encoding renders use unless told otherwise
+    uint32_t n_mats = 0;
+    uint32_t generation = 0;        // bumped whenever the BVH buffers are replaced
     crt_scene_info info{};
+
+    // Device view with the FP32 or the quantised nodes.
+    crt::DevScene view(bool f32) const {
+        crt::DevScene d = dev;
+        if (!f32) d.fnodes = nullptr;
+        return d;
+    }
     std::vector<uint32_t> lights;   // face indices in pick order
 };
 
-// Wavefront path-state buffers (see render.cu).
+// Wavefront path-state buffers (wavefront.cu).
 struct WaveBuffers {
     uint32_t capacity = 0;
-    crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, counters, waves, prof;
+    uint32_t seg_capacity = 0;      // wave segments the segs buffer holds
+    crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, counters, waves, segs, prof;
+    crt::DevBuf adj_L, adj_W, adj_shadow;   // adjoint replay state, allocated on first use
+};
+
+// One independent set of wavefront buffers with its own stream and captured
+// wave graph; several sets run waves concurrently (wavefront.cu).
+struct WaveSet {
+    WaveBuffers buf;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t acc_done = nullptr;   // recorded after this set's latest accumulate
+    void* graph = nullptr;
+    void* adj_graph = nullptr;        // adjoint wave body, captured for adj_key's pointers
+    const void* adj_key[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace crt {
-void destroy_wave_graph(void* g);
+void destroy_wave_sets(struct ::crt_render_s* r);
+void drop_wave_graphs(struct ::crt_render_s* r);
 }
+
+// One camera view of a render; its image is pixels
+// [pix_off, pix_off + width * height) of the render's accumulator.
+struct ViewState {
+    crt::Camera cam{};
+    uint32_t width = 0, height = 0;
+    uint32_t spp = 0;               // samples per pixel one batch render adds
+    uint32_t view_id = 0;           // Philox counter word
+    uint32_t pix_off = 0;
+    uint32_t samples_rendered = 0;
+    uint32_t npix() const { return width * height; }
+};
+
+// Samples [spp0, spp0 + nspp) of one view, rendered by a pass.
+struct ViewWork {
+    uint32_t spp0, nspp;
+};
 
 struct crt_render_s {
     crt_scene scene = nullptr;
-    crt::Camera cam{};
-    uint32_t width = 0, height = 0;
+    std::vector<ViewState> views;   // a single render has one; a batch many
     crt_render_options opts{};
-    uint32_t samples_rendered = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    crt::DevBuf accum, lut, ray_counts;
-    WaveBuffers wave;
-    void* wave_graph = nullptr;     // instantiated wave sequence (wavefront.cu)
-    ~crt_render_s() { crt::destroy_wave_graph(wave_graph); }
+    crt::DevBuf accum, lut, ray_counts, view_table;
+    std::vector<WaveSet> sets;
+    uint32_t scene_generation = 0;  // scene BVH the captured wave graphs point at
+    cudaEvent_t pass_start = nullptr;
+    ~crt_render_s() { crt::destroy_wave_sets(this); }
 };
+
+namespace crt {
+
+// Node encoding a render traverses: its option, else the scene's default.
+inline bool uses_f32_nodes(const crt_scene_s* s, int32_t node_format) {
+    if (!s->dev.fnodes) return false;
+    return node_format < 0 ? s->default_f32 : node_format == CRT_NODES_F32;
+}
+inline bool uses_f32_nodes(const crt_render_s* r) { return uses_f32_nodes(r->scene, r->opts.node_format); }
+
+// Traversal launch shape of a wavefront render.
+inline uint32_t traversal_block(const crt_render_options& o) { return o.block_size ? o.block_size : 128u; }
+inline uint32_t traversal_stack(const crt_render_options& o) { return o.stack_depth ? o.stack_depth : 16u; }
+inline uint32_t queue_chunk(const crt_render_options& o) { return o.queue_chunk ? o.queue_chunk : 32u; }
+
+// Checks the fields every render entry point shares; CRT_OK or an error.
+inline int check_render_options(const crt_render_options& o) {
+    if (o.max_depth == 0 || o.max_depth > 1024) return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
+    if (o.mode > CRT_MODE_WAVEFRONT) return set_error(CRT_ERR_INVALID, "unknown mode");
+    if (o.block_size != 0 && o.block_size != 64 && o.block_size != 128 && o.block_size != 256)
+        return set_error(CRT_ERR_INVALID, "block_size must be 0, 64, 128 or 256");
+    if (o.stack_depth != 0 && (o.stack_depth < 4 || o.stack_depth > (uint32_t)kStackSharedMax))
+        return set_error(CRT_ERR_INVALID, "stack_depth must be 0 or in [4, 32]");
+    if (o.node_format < -1 || o.node_format > CRT_NODES_F32) return set_error(CRT_ERR_INVALID, "unknown node format");
+    if (o.wave_sets > 8) return set_error(CRT_ERR_INVALID, "wave_sets must be in [0, 8]");
+    if (o.queue_chunk != 0 && o.queue_chunk != 32 && o.queue_chunk != 64 && o.queue_chunk != 128 &&
+        o.queue_chunk != 256)
+        return set_error(CRT_ERR_INVALID, "queue_chunk must be 0, 32, 64, 128 or 256");
+    return CRT_OK;
+}
+
+}  // namespace crt

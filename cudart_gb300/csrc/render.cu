@@ -5,14 +5,16 @@
 #include "crt_internal.h"
 #include "render_common.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
 namespace crt {
 
 int grid_for(uint32_t n, int block, int per_sm);
-int wavefront_pass(crt_render r, uint32_t spp0, uint32_t nspp);
-int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage_profile* out);
+int wavefront_pass(crt_render r, const std::vector<ViewWork>& work);
+int wavefront_profile_pass(crt_render r, const std::vector<ViewWork>& work, crt_stage_profile* out);
+int wavefront_adjoint(crt_render r, const std::vector<ViewWork>& work, const float4* adj, float* gkd, float* gka);
 
 constexpr int kMegaBlock = 128;         // 16 x 8 pixel tile, warps of 8 x 4
 constexpr uint32_t kMegaSppPerLaunch = 4;
@@ -24,8 +26,7 @@ template <bool F32>
 __global__ void __launch_bounds__(kMegaBlock) mega_kernel(RenderParams P) {
     __shared__ uint2 stack_sh[kStackShared * kMegaBlock];
     Stack st;
-    st.sh = stack_sh + threadIdx.x;
-    st.stride = kMegaBlock;
+    st.setup(stack_sh, kMegaBlock, kStackShared);
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t x = blockIdx.x * 16u + (warp & 1u) * 8u + (lane & 7u);
     const uint32_t y = blockIdx.y * 8u + (warp >> 1) * 4u + (lane >> 3);
@@ -85,19 +86,21 @@ Camera to_device_camera(const crt_camera& c) {
     return d;
 }
 
-RenderParams make_params(crt_render r, uint32_t spp0, uint32_t nspp) {
+RenderParams make_params(crt_render r, uint32_t view, uint32_t spp0, uint32_t nspp) {
+    const ViewState& V = r->views[view];
     RenderParams P;
-    P.S = r->scene->dev;
-    P.cam = r->cam;
-    P.accum = r->accum.as<float4>();
-    P.width = r->width;
-    P.height = r->height;
+    P.S = r->scene->view(uses_f32_nodes(r));
+    P.cam = V.cam;
+    P.accum = r->accum.as<float4>() + V.pix_off;
+    P.width = V.width;
+    P.height = V.height;
     P.seed = r->opts.seed;
-    P.view = r->opts.view_id;
+    P.view = V.view_id;
     P.spp0 = spp0;
     P.nspp = nspp;
     P.max_depth = r->opts.max_depth;
     P.ray_counts = r->ray_counts.as<unsigned long long>();
+    P.ka_scale = 3.0f * r->scene->dev.lights_area;
     return P;
 }
 
@@ -108,6 +111,134 @@ int check_device_error(crt_render r) {
     if (err & ERR_WATCHDOG) return set_error(CRT_ERR_WATCHDOG, "traversal exceeded its node-visit limit");
     if (err & ERR_STACK) return set_error(CRT_ERR_WATCHDOG, "traversal stack overflow");
     return CRT_OK;
+}
+
+// Copies the view table (cameras, sizes, accumulator offsets) to the device.
+static int upload_views(crt_render r) {
+    std::vector<DevView> t(r->views.size());
+    for (size_t v = 0; v < t.size(); ++v) {
+        const ViewState& V = r->views[v];
+        t[v].cam = V.cam;
+        t[v].width = V.width;
+        t[v].height = V.height;
+        t[v].view_id = V.view_id;
+        t[v].pix_off = V.pix_off;
+    }
+    CRT_CUDA(cudaMemcpyAsync(r->view_table.p, t.data(), t.size() * sizeof(DevView), cudaMemcpyHostToDevice,
+                             r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    return CRT_OK;
+}
+
+// A render handle over `views` (pixel offsets assigned here).
+static int create_render(crt_scene s, std::vector<ViewState> views, const crt_render_options* opts,
+                         crt_render* out) {
+    *out = nullptr;
+    crt_render_options o;
+    if (opts) o = *opts;
+    else crt_render_options_default(&o);
+    if (int st = check_render_options(o)) return st;
+    uint64_t total = 0;
+    for (ViewState& V : views) {
+        V.pix_off = (uint32_t)total;
+        total += (uint64_t)V.width * V.height;
+    }
+    if (total >= (1ull << 31)) return set_error(CRT_ERR_LIMIT, "views hold 2^31 pixels or more");
+    crt_render r = new crt_render_s();
+    r->scene = s;
+    r->views = std::move(views);
+    r->opts = o;
+    cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) r->own_stream = true;
+    if (e == cudaSuccess) e = r->accum.alloc(total * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->accum.p, 0, total * sizeof(float4), r->stream);
+    if (e == cudaSuccess) e = r->ray_counts.alloc(2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->ray_counts.p, 0, 2 * sizeof(unsigned long long), r->stream);
+    if (e == cudaSuccess) e = r->view_table.alloc(r->views.size() * sizeof(DevView));
+    // gammaCorrectPixel (renderer.cu:495-504) runs on the host in the
+    // reference; the same powf per byte value gives the table.
+    uint8_t lut[256];
+    const float inv_gamma = 1.f / 2.2f;
+    for (int v = 0; v < 256; ++v) lut[v] = (uint8_t)(powf((float)v * 1.f / 255.f, inv_gamma) * 255.f);
+    if (e == cudaSuccess) e = r->lut.alloc(256);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->lut.p, lut, 256, cudaMemcpyHostToDevice, r->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+    int st = e == cudaSuccess ? upload_views(r) : cuda_error(e, "crt_render_create");
+    if (st != CRT_OK) {
+        if (r->own_stream) cudaStreamDestroy(r->stream);
+        r->stream = nullptr;
+        delete r;
+        return st;
+    }
+    *out = r;
+    return CRT_OK;
+}
+
+// Renders work[v] of every view: the wavefront form as one stream of waves
+// over all views, the megakernel as one launch sequence per view.
+static int run_pass(crt_render r, const std::vector<ViewWork>& work, crt_stage_profile* prof) {
+    bool any = false;
+    for (size_t v = 0; v < work.size(); ++v) {
+        if ((uint64_t)work[v].spp0 + work[v].nspp >= (1ull << 32))
+            return set_error(CRT_ERR_LIMIT, "sample counter overflow");
+        any = any || work[v].nspp;
+    }
+    if (!any) return CRT_OK;
+    if (prof) {
+        if (int st = wavefront_profile_pass(r, work, prof)) return st;
+    } else if (r->opts.mode == CRT_MODE_WAVEFRONT) {
+        if (int st = wavefront_pass(r, work)) return st;
+    } else {
+        const bool f32 = uses_f32_nodes(r);
+        for (uint32_t v = 0; v < (uint32_t)work.size(); ++v) {
+            const ViewState& V = r->views[v];
+            const dim3 grid((V.width + 15) / 16, (V.height + 7) / 8);
+            for (uint32_t done = 0; done < work[v].nspp;) {
+                const uint32_t k = std::min(work[v].nspp - done, kMegaSppPerLaunch);
+                const RenderParams P = make_params(r, v, work[v].spp0 + done, k);
+                if (f32) mega_kernel<true><<<grid, kMegaBlock, 0, r->stream>>>(P);
+                else mega_kernel<false><<<grid, kMegaBlock, 0, r->stream>>>(P);
+                done += k;
+            }
+        }
+        CRT_CUDA(cudaGetLastError());
+    }
+    for (size_t v = 0; v < work.size(); ++v) r->views[v].samples_rendered += work[v].nspp;
+    return CRT_OK;
+}
+
+static std::vector<ViewWork> uniform_work(crt_render r, uint32_t n_spp) {
+    std::vector<ViewWork> w;
+    for (const ViewState& V : r->views) w.push_back({V.samples_rendered, n_spp});
+    return w;
+}
+
+static int resolve_view(crt_render r, uint32_t v, uint8_t* host_rgba) {
+    const ViewState& V = r->views[v];
+    if (V.samples_rendered == 0) return set_error(CRT_ERR_INVALID, "no samples rendered");
+    const uint32_t n = V.npix();
+    DevBuf out;
+    CRT_CUDA(out.alloc((size_t)n * 4));
+    resolve_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>() + V.pix_off, n,
+                                                              (float)V.samples_rendered,
+                                                              r->lut.as<uint8_t>(), out.as<uchar4>());
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaMemcpyAsync(host_rgba, out.p, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    return check_device_error(r);
+}
+
+static int accum_view(crt_render r, uint32_t v, float* host_rgb) {
+    const ViewState& V = r->views[v];
+    const uint32_t n = V.npix();
+    DevBuf out;
+    CRT_CUDA(out.alloc((size_t)n * 12));
+    unpack_accum_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>() + V.pix_off, n,
+                                                                   out.as<float>());
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaMemcpyAsync(host_rgb, out.p, (size_t)n * 12, cudaMemcpyDeviceToHost, r->stream));
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    return check_device_error(r);
 }
 
 }  // namespace crt
@@ -125,6 +256,7 @@ void crt_render_options_default(crt_render_options* o) {
     o->mode = CRT_MODE_MEGAKERNEL;
     o->block_size = 0;
     o->wave_paths = 0;
+    o->node_format = -1;        // the scene's default encoding
 }
 
 int crt_render_create(crt_scene s, const crt_camera* cam, uint32_t width, uint32_t height,
@@ -132,42 +264,31 @@ int crt_render_create(crt_scene s, const crt_camera* cam, uint32_t width, uint32
     if (!s || !cam || !out) return set_error(CRT_ERR_INVALID, "crt_render_create: null argument");
     if (width == 0 || height == 0 || (uint64_t)width * height >= (1ull << 31))
         return set_error(CRT_ERR_INVALID, "crt_render_create: bad image size");
-    *out = nullptr;
-    crt_render r = new crt_render_s();
-    r->scene = s;
-    r->width = width;
-    r->height = height;
-    if (opts) r->opts = *opts;
-    else crt_render_options_default(&r->opts);
-    if (r->opts.max_depth == 0 || r->opts.max_depth > 1024) {
-        delete r;
-        return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
+    std::vector<ViewState> views(1);
+    views[0].cam = to_device_camera(*cam);
+    views[0].width = width;
+    views[0].height = height;
+    views[0].view_id = opts ? opts->view_id : 0;
+    return create_render(s, std::move(views), opts, out);
+}
+
+int crt_batch_create(crt_scene s, const crt_view* views, uint32_t num_views, const crt_render_options* opts,
+                     crt_render* out) {
+    if (!s || !views || !out) return set_error(CRT_ERR_INVALID, "crt_batch_create: null argument");
+    if (num_views == 0 || num_views > CRT_MAX_VIEWS)
+        return set_error(CRT_ERR_LIMIT, "crt_batch_create: num_views must be in [1, CRT_MAX_VIEWS]");
+    std::vector<ViewState> vs(num_views);
+    for (uint32_t v = 0; v < num_views; ++v) {
+        const crt_view& d = views[v];
+        if (d.width == 0 || d.height == 0 || (uint64_t)d.width * d.height >= (1ull << 31))
+            return set_error(CRT_ERR_INVALID, "crt_batch_create: bad image size in view " + std::to_string(v));
+        vs[v].cam = to_device_camera(d.camera);
+        vs[v].width = d.width;
+        vs[v].height = d.height;
+        vs[v].spp = d.spp;
+        vs[v].view_id = d.view_id;
     }
-    if (r->opts.mode > CRT_MODE_WAVEFRONT) { delete r; return set_error(CRT_ERR_INVALID, "unknown mode"); }
-    r->cam = to_device_camera(*cam);
-    const uint64_t npix = (uint64_t)width * height;
-    cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) r->own_stream = true;
-    if (e == cudaSuccess) e = r->accum.alloc(npix * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMemsetAsync(r->accum.p, 0, npix * sizeof(float4), r->stream);
-    if (e == cudaSuccess) e = r->ray_counts.alloc(2 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMemsetAsync(r->ray_counts.p, 0, 2 * sizeof(unsigned long long), r->stream);
-    // gammaCorrectPixel (renderer.cu:495-504) runs on the host in the
-    // reference; the same powf per byte value gives the table.
-    uint8_t lut[256];
-    const float inv_gamma = 1.f / 2.2f;
-    for (int v = 0; v < 256; ++v) lut[v] = (uint8_t)(powf((float)v * 1.f / 255.f, inv_gamma) * 255.f);
-    if (e == cudaSuccess) e = r->lut.alloc(256);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(r->lut.p, lut, 256, cudaMemcpyHostToDevice, r->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
-    if (e != cudaSuccess) {
-        int st = cuda_error(e, "crt_render_create");
-        if (r->own_stream) cudaStreamDestroy(r->stream);
-        delete r;
-        return st;
-    }
-    *out = r;
-    return CRT_OK;
+    return create_render(s, std::move(vs), opts, out);
 }
 
 int crt_render_destroy(crt_render r) {
@@ -184,40 +305,27 @@ int crt_render_set_stream(crt_render r, void* stream) {
     if (r->own_stream) cudaStreamDestroy(r->stream);
     r->stream = (cudaStream_t)stream;
     r->own_stream = false;
-    destroy_wave_graph(r->wave_graph);
-    r->wave_graph = nullptr;
     return CRT_OK;
 }
 
 int crt_render_set_camera(crt_render r, const crt_camera* cam) {
     if (!r || !cam) return set_error(CRT_ERR_INVALID, "null argument");
-    CRT_CUDA(cudaStreamSynchronize(r->stream));
-    r->cam = to_device_camera(*cam);
-    destroy_wave_graph(r->wave_graph);   // the captured launches hold the old camera
-    r->wave_graph = nullptr;
-    return CRT_OK;
+    CRT_CUDA(cudaStreamSynchronize(r->stream));   // every wave set joins this stream
+    r->views[0].cam = to_device_camera(*cam);
+    return upload_views(r);   // the wave kernels read cameras from the view table
 }
 
 int crt_render_pass(crt_render r, uint32_t n_spp) {
     if (!r) return set_error(CRT_ERR_INVALID, "null render");
     if (n_spp == 0) return CRT_OK;
-    if ((uint64_t)r->samples_rendered + n_spp >= (1ull << 32))
-        return set_error(CRT_ERR_LIMIT, "sample counter overflow");
-    if (r->opts.mode == CRT_MODE_WAVEFRONT) {
-        int st = wavefront_pass(r, r->samples_rendered, n_spp);
-        if (st != CRT_OK) return st;
-    } else {
-        dim3 grid((r->width + 15) / 16, (r->height + 7) / 8);
-        for (uint32_t done = 0; done < n_spp;) {
-            uint32_t k = n_spp - done < kMegaSppPerLaunch ? n_spp - done : kMegaSppPerLaunch;
-            if (r->scene->dev.fnodes) mega_kernel<true><<<grid, kMegaBlock, 0, r->stream>>>(make_params(r, r->samples_rendered + done, k));
-            else mega_kernel<false><<<grid, kMegaBlock, 0, r->stream>>>(make_params(r, r->samples_rendered + done, k));
-            done += k;
-        }
-        CRT_CUDA(cudaGetLastError());
-    }
-    r->samples_rendered += n_spp;
-    return CRT_OK;
+    return run_pass(r, uniform_work(r, n_spp), nullptr);
+}
+
+int crt_batch_render(crt_render r) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    std::vector<ViewWork> w;
+    for (const ViewState& V : r->views) w.push_back({V.samples_rendered, V.spp});
+    return run_pass(r, w, nullptr);
 }
 
 int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out) {
@@ -226,17 +334,39 @@ int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out
         return set_error(CRT_ERR_UNSUPPORTED, "stage profiling needs a wavefront handle");
     std::memset(out, 0, sizeof(*out));
     if (n_spp == 0) return CRT_OK;
-    if ((uint64_t)r->samples_rendered + n_spp >= (1ull << 32))
-        return set_error(CRT_ERR_LIMIT, "sample counter overflow");
-    int st = wavefront_profile_pass(r, r->samples_rendered, n_spp, out);
-    if (st != CRT_OK) return st;
-    r->samples_rendered += n_spp;
-    return CRT_OK;
+    return run_pass(r, uniform_work(r, n_spp), out);
+}
+
+int crt_render_adjoint(crt_render r, uint32_t spp0, uint32_t n_spp, const float* d_adjoint, float* d_grad_kd,
+                       float* d_grad_ka) {
+    if (!r || !d_adjoint || !d_grad_kd || !d_grad_ka) return set_error(CRT_ERR_INVALID, "crt_render_adjoint: null argument");
+    if (((uintptr_t)d_adjoint & 15u) != 0) return set_error(CRT_ERR_INVALID, "d_adjoint must be 16-byte aligned");
+    if (n_spp == 0) return CRT_OK;
+    if ((uint64_t)spp0 + n_spp >= (1ull << 32)) return set_error(CRT_ERR_LIMIT, "sample index overflow");
+    std::vector<ViewWork> work(r->views.size(), ViewWork{spp0, n_spp});
+    return wavefront_adjoint(r, work, reinterpret_cast<const float4*>(d_adjoint), d_grad_kd, d_grad_ka);
 }
 
 int crt_render_samples_rendered(crt_render r, uint32_t* out) {
     if (!r || !out) return set_error(CRT_ERR_INVALID, "null argument");
-    *out = r->samples_rendered;
+    *out = r->views[0].samples_rendered;
+    return CRT_OK;
+}
+
+int crt_render_view_info(crt_render r, uint32_t view, crt_view* desc, uint32_t* samples_rendered,
+                         uint32_t* pixel_offset) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    if (view >= r->views.size()) return set_error(CRT_ERR_INVALID, "view index out of range");
+    const ViewState& V = r->views[view];
+    if (desc) {
+        std::memset(desc, 0, sizeof(*desc));
+        desc->width = V.width;
+        desc->height = V.height;
+        desc->spp = V.spp;
+        desc->view_id = V.view_id;
+    }
+    if (samples_rendered) *samples_rendered = V.samples_rendered;
+    if (pixel_offset) *pixel_offset = V.pix_off;
     return CRT_OK;
 }
 
@@ -248,34 +378,29 @@ int crt_render_synchronize(crt_render r) {
 
 int crt_render_resolve(crt_render r, uint8_t* host_rgba) {
     if (!r || !host_rgba) return set_error(CRT_ERR_INVALID, "null argument");
-    if (r->samples_rendered == 0) return set_error(CRT_ERR_INVALID, "no samples rendered");
-    const uint32_t n = r->width * r->height;
-    DevBuf out;
-    CRT_CUDA(out.alloc((size_t)n * 4));
-    resolve_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>(), n,
-                                                              (float)r->samples_rendered,
-                                                              r->lut.as<uint8_t>(), out.as<uchar4>());
-    CRT_CUDA(cudaGetLastError());
-    CRT_CUDA(cudaMemcpyAsync(host_rgba, out.p, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
-    CRT_CUDA(cudaStreamSynchronize(r->stream));
-    return check_device_error(r);
+    return resolve_view(r, 0, host_rgba);
+}
+
+int crt_render_view_resolve(crt_render r, uint32_t view, uint8_t* host_rgba) {
+    if (!r || !host_rgba) return set_error(CRT_ERR_INVALID, "null argument");
+    if (view >= r->views.size()) return set_error(CRT_ERR_INVALID, "view index out of range");
+    return resolve_view(r, view, host_rgba);
 }
 
 int crt_render_accum(crt_render r, float* host_rgb) {
     if (!r || !host_rgb) return set_error(CRT_ERR_INVALID, "null argument");
-    const uint32_t n = r->width * r->height;
-    DevBuf out;
-    CRT_CUDA(out.alloc((size_t)n * 12));
-    unpack_accum_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>(), n, out.as<float>());
-    CRT_CUDA(cudaGetLastError());
-    CRT_CUDA(cudaMemcpyAsync(host_rgb, out.p, (size_t)n * 12, cudaMemcpyDeviceToHost, r->stream));
-    CRT_CUDA(cudaStreamSynchronize(r->stream));
-    return check_device_error(r);
+    return accum_view(r, 0, host_rgb);
+}
+
+int crt_render_view_accum(crt_render r, uint32_t view, float* host_rgb) {
+    if (!r || !host_rgb) return set_error(CRT_ERR_INVALID, "null argument");
+    if (view >= r->views.size()) return set_error(CRT_ERR_INVALID, "view index out of range");
+    return accum_view(r, view, host_rgb);
 }
 
 int crt_render_accum_device(crt_render r, float** d_rgb) {
     if (!r || !d_rgb) return set_error(CRT_ERR_INVALID, "null argument");
-    *d_rgb = r->accum.as<float>();   // [n][4]: rgb + unused
+    *d_rgb = r->accum.as<float>();   // [pixels of every view][4]: rgb + unused
     return CRT_OK;
 }
 
@@ -283,7 +408,7 @@ int crt_render_reset(crt_render r) {
     if (!r) return set_error(CRT_ERR_INVALID, "null render");
     CRT_CUDA(cudaMemsetAsync(r->accum.p, 0, r->accum.bytes, r->stream));
     CRT_CUDA(cudaMemsetAsync(r->ray_counts.p, 0, r->ray_counts.bytes, r->stream));
-    r->samples_rendered = 0;
+    for (ViewState& V : r->views) V.samples_rendered = 0;
     return CRT_OK;
 }
 

@@ -26,6 +26,16 @@ struct RenderParams {
     uint32_t spp0, nspp;
     uint32_t max_depth;
     unsigned long long* ray_counts;   // [0] extension rays, [1] shadow rays
+    float ka_scale;                   // d(stored emission)/d(material ka) = 3 * lights area
+};
+
+// One camera view of a render as the wavefront kernels see it: its image
+// is pixels [pix_off, pix_off + width * height) of the render's accumulator.
+struct DevView {
+    Camera cam;
+    uint32_t width, height;
+    uint32_t view_id;    // Philox counter word
+    uint32_t pix_off;
 };
 
 struct PathState {
@@ -41,12 +51,29 @@ struct ShadowReq {
     float t_light;
     uint32_t light_face;
     float3 contrib;      // mask * directLighting if the light is visible
+    float3 dcontrib;     // adjoint only: d contrib / d (light material ka), per channel
+    uint32_t light_mat;  // adjoint only
 };
 
-CRT_D void begin_path(const RenderParams& P, uint32_t x, uint32_t y, uint32_t pixel, uint32_t sample,
-                      PathState& ps, Ray& ray) {
-    ps.rng.init(P.seed, P.view, pixel, sample);
-    ray = camera_ray(P.cam, (int)x, (int)y, ps.rng);
+// Gradient hooks of shade_hit.  The forward estimator uses NoGrad (every
+// hook compiles away); the adjoint replay passes a policy that turns each
+// event into gradient contributions (path-replay backpropagation):
+// * emission(m, d): the path just added mask * ka_m / lights_area;
+//   d = d(that term)/d(material ka), channel-wise;
+// * albedo(m, kd, color): a diffuse vertex of untextured material m is about
+//   to multiply the throughput by kd; everything the path adds from here on
+//   (its total minus `color`, the radiance so far) carries one factor kd.
+// Russian roulette's survival probability is treated as a constant.
+struct NoGrad {
+    static constexpr bool kActive = false;
+    CRT_D void emission(uint32_t, float3) {}
+    CRT_D void albedo(uint32_t, float3, float3) {}
+};
+
+CRT_D void begin_path(const Camera& cam, uint64_t seed, uint32_t view, uint32_t x, uint32_t y, uint32_t pixel,
+                      uint32_t sample, PathState& ps, Ray& ray) {
+    ps.rng.init(seed, view, pixel, sample);
+    ray = camera_ray(cam, (int)x, (int)y, ps.rng);
     ps.color = f3(0.f, 0.f, 0.f);
     ps.mask = f3(1.f, 1.f, 1.f);
     ps.prev = DIFFUSE;
@@ -60,13 +87,16 @@ CRT_D void shade_miss(PathState& ps) {
 
 // One bounce after a hit.  Updates ps and `ray` (the next extension ray)
 // and returns whether the path continues (Russian roulette, renderer.cu:252-259).
-CRT_D bool shade_hit(const RenderParams& P, PathState& ps, Ray& ray, const Hit& h, ShadowReq& sr) {
+template <class G = NoGrad>
+CRT_D bool shade_hit(const RenderParams& P, PathState& ps, Ray& ray, const Hit& h, ShadowReq& sr, G* g = nullptr) {
     const DevScene& S = P.S;
     sr.valid = false;
     const Shading sh = load_shading(S, (uint32_t)h.face);
     const Material m = load_material(S, sh.material);
-    if (ps.bounce == 0 || ps.prev == SPECULAR || ps.prev == REFRACTIVE)
+    if (ps.bounce == 0 || ps.prev == SPECULAR || ps.prev == REFRACTIVE) {
         ps.color = ps.color + ps.mask * m.ka * (1.f / S.lights_area);
+        if (G::kActive) g->emission(sh.material, ps.mask * P.ka_scale * (1.f / S.lights_area));
+    }
     const float3 normal = shading_normal(sh, h.u, h.v);
     const float3 position = ray.o + ray.d * h.t + normal * kEps2;
     const float3 out_dir = normalize(ray.d);
@@ -107,6 +137,8 @@ CRT_D bool shade_hit(const RenderParams& P, PathState& ps, Ray& ray, const Hit& 
             const float tu = uv01.x * w + uv01.z * h.u + uv2.x * h.v;
             const float tv = uv01.y * w + uv01.w * h.u + uv2.y * h.v;
             kd = sample_texture(S, m.tex, tu, tv);
+        } else if (G::kActive) {
+            g->albedo(sh.material, kd, ps.color);
         }
         ps.mask = ps.mask * (kd * cosw) / 0.5f;
         const LightGeo L = load_light(S, pick_light(S, ps.rng.next()));
@@ -124,7 +156,12 @@ CRT_D bool shade_hit(const RenderParams& P, PathState& ps, Ray& ray, const Hit& 
                 sr.d = sd;
                 sr.t_light = tl;
                 sr.light_face = L.face;
-                sr.contrib = ps.mask * light_contribution(S, L, lcolor, tl, lu, lv, sd);
+                const float wgt = light_weight(S, L, tl, lu, lv, sd);
+                sr.contrib = ps.mask * (f3(0.f, 0.f, 0.f) + lcolor * wgt);
+                if (G::kActive) {
+                    sr.dcontrib = ps.mask * (P.ka_scale * wgt);
+                    sr.light_mat = L.material;
+                }
             }
         }
     }
@@ -158,7 +195,7 @@ CRT_D float3 sample_path(const RenderParams& P, int x, int y, uint32_t pixel, ui
                          uint32_t& n_ext, uint32_t& n_shadow) {
     PathState ps;
     Ray ray;
-    begin_path(P, (uint32_t)x, (uint32_t)y, pixel, sample, ps, ray);
+    begin_path(P.cam, P.seed, P.view, (uint32_t)x, (uint32_t)y, pixel, sample, ps, ray);
     for (uint32_t bounce = 0; bounce < P.max_depth; ++bounce) {
         Hit h;
         h.t = FLT_MAX;

@@ -40,6 +40,32 @@ int upload(DevBuf& b, const std::vector<T>& v) {
     return CRT_OK;
 }
 
+// Uploads a built BVH (both node encodings while child indices fit 24 bits)
+// and points the device view and the statistics at it.  The buffers it
+// replaces are freed on return: callers make sure no work still reads them.
+static int install_bvh(crt_scene s, Bvh8& b, uint32_t width) {
+    DevBuf nodes, fnodes, tris;
+    int st = CRT_OK;
+    if (b.fnodes_ok && (st = upload(fnodes, b.fnodes))) return st;
+    if ((st = upload(nodes, b.nodes)) || (st = upload(tris, b.tris))) return st;
+    s->nodes.swap(nodes);
+    s->fnodes.swap(fnodes);
+    s->tris.swap(tris);
+    s->bvh = std::move(b);
+    s->dev.nodes = s->nodes.as<float4>();
+    s->dev.fnodes = s->bvh.fnodes_ok ? s->fnodes.as<float4>() : nullptr;
+    s->dev.tris = s->tris.as<float4>();
+    crt_scene_info& I = s->info;
+    I.num_nodes = (uint32_t)s->bvh.nodes.size();
+    I.max_depth = s->bvh.max_depth;
+    I.node_bytes = s->default_f32 ? s->bvh.fnodes.size() * sizeof(Bvh8FloatNode)
+                                  : s->bvh.nodes.size() * sizeof(Bvh8Node);
+    I.triangle_bytes = s->bvh.tris.size() * sizeof(TriRecord);
+    I.bvh_width = width;
+    ++s->generation;
+    return CRT_OK;
+}
+
 inline float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
 inline float bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline float bits(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
@@ -104,6 +130,8 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     if (d->num_textures && (!d->texture_dims || !d->texels))
         return set_error(CRT_ERR_INVALID, "textures need dims and texels");
     if (d->node_format > CRT_NODES_F32) return set_error(CRT_ERR_INVALID, "unknown node format");
+    if (d->bvh_width != 0 && d->bvh_width != 4 && d->bvh_width != 8)
+        return set_error(CRT_ERR_INVALID, "bvh_width must be 4 or 8");
 
     auto t0 = std::chrono::steady_clock::now();
     crt_scene s = new crt_scene_s();
@@ -144,7 +172,9 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     if (dev_err != cudaSuccess) { delete s; return cuda_error(dev_err, "cudaGetDevice"); }
 
     const char* msg = nullptr;
-    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, s->bvh, &msg)) {
+    const uint32_t width = d->bvh_width ? d->bvh_width : 8u;
+    Bvh8 bvh;
+    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, bvh, &msg, (int)width)) {
         delete s;
         return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
     }
@@ -205,15 +235,15 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
     int st = CRT_OK;
     const bool f32 = d->node_format == CRT_NODES_F32;
-    if (f32 && !s->bvh.fnodes_ok) {
+    if (f32 && !bvh.fnodes_ok) {
         delete s;
         return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
     }
-    if (f32 && (st = upload(s->fnodes, s->bvh.fnodes))) {
-        delete s;
-        return st;
-    }
-    if ((st = upload(s->nodes, s->bvh.nodes)) || (st = upload(s->tris, s->bvh.tris)) ||
+    // Both encodings go to the device (the FP32 one only while child indices
+    // fit 24 bits); each render picks one.
+    s->default_f32 = f32;
+    s->n_mats = d->num_materials;
+    if ((st = install_bvh(s, bvh, width)) ||
         (st = upload(s->shade, shade)) || (st = upload(s->uvs, uvs)) || (st = upload(s->mats, mats)) ||
         (st = upload(s->light_geo, lgeo)) || (st = upload(s->texels, texels)) ||
         (st = upload(s->tex_dims, dims)) || (st = upload(s->tex_offsets, offs))) {
@@ -225,9 +255,6 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     if (e != cudaSuccess) { delete s; return cuda_error(e, "error word"); }
 
     DevScene& D = s->dev;
-    D.nodes = s->nodes.as<float4>();
-    D.fnodes = f32 ? s->fnodes.as<float4>() : nullptr;
-    D.tris = s->tris.as<float4>();
     D.shade = s->shade.as<float4>();
     D.uvs = s->uvs.as<float4>();
     D.mats = s->mats.as<float4>();
@@ -243,13 +270,9 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
     crt_scene_info& I = s->info;
     I.num_triangles = n;
-    I.num_nodes = (uint32_t)s->bvh.nodes.size();
-    I.max_depth = s->bvh.max_depth;
     I.num_lights = D.n_lights;
     I.num_materials = d->num_materials;
     I.num_textures = d->num_textures;
-    I.node_bytes = f32 ? s->bvh.fnodes.size() * sizeof(Bvh8FloatNode) : s->bvh.nodes.size() * sizeof(Bvh8Node);
-    I.triangle_bytes = s->bvh.tris.size() * sizeof(TriRecord);
     I.shading_bytes = (shade.size() + uvs.size()) * sizeof(float4);
     I.texture_bytes = texels.size() * sizeof(float4);
     I.lights_area = lights_area;
@@ -260,6 +283,36 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
 int crt_scene_destroy(crt_scene s) {
     delete s;
+    return CRT_OK;
+}
+
+int crt_scene_set_bvh_width(crt_scene s, uint32_t width) {
+    if (!s) return set_error(CRT_ERR_INVALID, "crt_scene_set_bvh_width: null scene");
+    if (width != 4 && width != 8) return set_error(CRT_ERR_INVALID, "bvh_width must be 4 or 8");
+    if (width == s->info.bvh_width) return CRT_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    // the triangle records hold each face's v1, e1, e2 exactly as built
+    const uint32_t n = s->info.num_triangles;
+    std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n);
+    for (const TriRecord& r : s->bvh.tris) {
+        const uint32_t f = r.face;
+        for (int k = 0; k < 3; ++k) {
+            v1[3ull * f + k] = r.v1[k];
+            e1[3ull * f + k] = r.e1[k];
+            e2[3ull * f + k] = r.e2[k];
+        }
+    }
+    Bvh8 bvh;
+    const char* msg = nullptr;
+    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, bvh, &msg, (int)width))
+        return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
+    if (s->default_f32 && !bvh.fnodes_ok)
+        return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; rebuilt BVH has more than 2^24 nodes");
+    CRT_CUDA(cudaSetDevice(s->device));
+    CRT_CUDA(cudaDeviceSynchronize());   // nothing may still read the old nodes
+    int st = install_bvh(s, bvh, width);
+    if (st != CRT_OK) return st;
+    s->info.build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return CRT_OK;
 }
 
@@ -276,9 +329,11 @@ int crt_scene_export_bvh(crt_scene s, void* nodes, void* triangles) {
     return CRT_OK;
 }
 
-int crt_bvh_build_host(const float* positions, uint32_t n, uint32_t* num_nodes,
+int crt_bvh_build_host(const float* positions, uint32_t n, uint32_t bvh_width, uint32_t* num_nodes,
                        uint32_t* max_depth, void* nodes, void* triangles) {
     if (!positions || n == 0) return set_error(CRT_ERR_INVALID, "crt_bvh_build_host: no triangles");
+    if (bvh_width != 0 && bvh_width != 4 && bvh_width != 8)
+        return set_error(CRT_ERR_INVALID, "bvh_width must be 4 or 8");
     std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n);
     for (uint32_t i = 0; i < n; ++i)
         for (int k = 0; k < 3; ++k) {
@@ -289,7 +344,8 @@ int crt_bvh_build_host(const float* positions, uint32_t n, uint32_t* num_nodes,
         }
     Bvh8 b;
     const char* msg = nullptr;
-    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, b, &msg))
+    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, b, &msg,
+                    bvh_width ? (int)bvh_width : 8))
         return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
     if (num_nodes) *num_nodes = (uint32_t)b.nodes.size();
     if (max_depth) *max_depth = b.max_depth;

@@ -19,8 +19,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_closest_kernel(DevScene S, 
                                                                     uint32_t* __restrict__ out_tris) {
     __shared__ uint2 stack_sh[kStackShared * kTraceBlock];
     Stack st;
-    st.sh = stack_sh + threadIdx.x;
-    st.stride = kTraceBlock;
+    st.setup(stack_sh, kTraceBlock, kStackShared);
     for (uint32_t i = blockIdx.x * kTraceBlock + threadIdx.x; i < n; i += gridDim.x * kTraceBlock) {
         const float4 a = rays[2ull * i], b = rays[2ull * i + 1];
         Hit h;
@@ -65,9 +64,9 @@ int crt_trace_closest(crt_scene s, const float* d_rays, uint32_t n, int32_t* d_i
         return set_error(CRT_ERR_INVALID, "crt_trace_closest: null argument");
     if (n == 0) return CRT_OK;
     if (((uintptr_t)d_rays & 15u) != 0) return set_error(CRT_ERR_INVALID, "rays must be 16-byte aligned");
-    auto k = s->dev.fnodes ? trace_closest_kernel<false, true> : trace_closest_kernel<false, false>;
+    auto k = s->default_f32 ? trace_closest_kernel<false, true> : trace_closest_kernel<false, false>;
     k<<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
-        s->dev, (const float4*)d_rays, n, d_index, d_t, (float2*)d_uv, nullptr, nullptr);
+        s->view(s->default_f32), (const float4*)d_rays, n, d_index, d_t, (float2*)d_uv, nullptr, nullptr);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
 }
@@ -78,9 +77,9 @@ int crt_trace_counts(crt_scene s, const float* d_rays, uint32_t n, uint32_t* d_n
         return set_error(CRT_ERR_INVALID, "crt_trace_counts: null argument");
     if (n == 0) return CRT_OK;
     if (((uintptr_t)d_rays & 15u) != 0) return set_error(CRT_ERR_INVALID, "rays must be 16-byte aligned");
-    auto k = s->dev.fnodes ? trace_closest_kernel<true, true> : trace_closest_kernel<true, false>;
+    auto k = s->default_f32 ? trace_closest_kernel<true, true> : trace_closest_kernel<true, false>;
     k<<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
-        s->dev, (const float4*)d_rays, n, nullptr, nullptr, nullptr, d_nodes, d_tris);
+        s->view(s->default_f32), (const float4*)d_rays, n, nullptr, nullptr, nullptr, d_nodes, d_tris);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
 }

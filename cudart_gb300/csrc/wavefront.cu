@@ -1,7 +1,9 @@
 // wavefront.cu -- the wavefront form of the path tracer.
 //
-// A pass is cut into waves of at most `capacity` paths (a pixel range x a
-// sample range).  One wave runs
+// A pass is cut into waves of at most `capacity` paths.  A wave is a list of
+// segments, each a pixel range x a sample range of one view (a single render
+// has one view; a batch many), and holds each pixel of a view at most once.
+// One wave runs
 //
 //   generate -> { extend -> shade -> shadow -> flip } x max_depth -> accumulate
 //
@@ -30,10 +32,12 @@
 namespace crt {
 
 int grid_for(uint32_t n, int block, int per_sm);
-RenderParams make_params(crt_render r, uint32_t spp0, uint32_t nspp);
+RenderParams make_params(crt_render r, uint32_t view, uint32_t spp0, uint32_t nspp);
 
-constexpr int kWaveBlock = 128;
+constexpr int kWaveBlock = 128;            // generate / shade / counting kernels
+constexpr int kTraversalBlockMax = 256;    // extend / shadow: block size chosen at launch
 constexpr uint32_t kDefaultCapacity = 1u << 22;
+constexpr uint32_t kDefaultWaveSets = 3;
 constexpr uint32_t kMaxWaves = 1u << 16;   // descriptors uploaded per chunk
 
 enum Counter : uint32_t {
@@ -51,28 +55,119 @@ enum Counter : uint32_t {
 // Profiling totals: extension rays, nodes, triangles; shadow rays, nodes, triangles.
 enum ProfileCounter : uint32_t { P_EXT_RAYS, P_EXT_NODES, P_EXT_TRIS, P_SHD_RAYS, P_SHD_NODES, P_SHD_TRIS, P_COUNT };
 
+// Pixels [p0, p1) x samples [s0, s1) of view `view`: path slot0 + k * (p1 -
+// p0) + (p - p0) carries sample s0 + k of pixel p; the segment's pixels are
+// entries [pix0, pix0 + p1 - p0) of the wave's accumulate range.
+struct WaveSeg {
+    uint32_t view, p0, p1, s0, s1, slot0, pix0, pad;
+};
+
+// Path state word st_m.w: previous bsdf (8 bits), bounce (11 bits), view.
+constexpr uint32_t kBounceShift = 8, kViewShift = 19;
+
 struct WaveParams {
-    RenderParams R;
-    float4* st_o;       // o.xyz, pixel
+    RenderParams R;     // scene, seed, depth, ray counts; R.accum = all views
+    const DevView* views;
+    float4* st_o;       // o.xyz, pixel within its view
     float4* st_d;       // d.xyz, sample
     float4* st_c;       // color.xyz, rng draws
-    float4* st_m;       // mask.xyz, prev | bounce << 8
+    float4* st_m;       // mask.xyz, prev | bounce << 8 | view << 19
     float4* hit;        // t, face, u, v
     uint32_t* queue[2];
     float4* shadow;     // 3 float4 per request
     uint32_t* counters;
-    const uint4* waves; // pixel0, pixel1, sample0, sample1
+    const uint4* waves; // first segment, segments, paths, accumulate entries
+    const WaveSeg* segs;
     unsigned long long* prof;   // ProfileCounter totals (profiling pass only)
+    int stack_depth;            // traversal stack entries in shared memory
+    uint32_t queue_chunk;       // queue entries a warp claims per fetch (batch mode)
+    // adjoint replay only
+    const float4* adj;          // d(objective)/d(radiance sum), per pixel of every view
+    float4* st_L;               // radiance of each path's primal trace
+    float4* st_W;               // adjoint weight of each path's pixel
+    float4* shd_grad;           // per shadow request: w * d contrib / d ka, light material
+    float* grad_kd;             // [n_mats][3], added to
+    float* grad_ka;             // [n_mats][3], added to
+    uint32_t n_mats;
+};
+
+// ---------------------------------------------------------------------------
+// Adjoint (path-replay backpropagation) helpers.  Gradients are summed per
+// block in shared memory, [n_mats][6] = kd rgb, ka rgb; within a warp the
+// lanes adding to the same material are summed first, so each warp issues
+// one shared atomic per material and channel.
+// ---------------------------------------------------------------------------
+CRT_D void warp_add_grad(float* acc, uint32_t key, uint32_t off, float3 v) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, key);
+    float3 s = f3(0.f, 0.f, 0.f);
+    for (uint32_t rest = active; rest; rest &= rest - 1u) {
+        const int j = __ffs(rest) - 1;
+        const float x = __shfl_sync(active, v.x, j);
+        const float y = __shfl_sync(active, v.y, j);
+        const float z = __shfl_sync(active, v.z, j);
+        if ((peers >> j) & 1u) s = s + f3(x, y, z);
+    }
+    if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
+        float* a = acc + 6u * key + off;
+        atomicAdd(a, s.x);
+        atomicAdd(a + 1, s.y);
+        atomicAdd(a + 2, s.z);
+    }
+}
+
+CRT_D void zero_grad_block(float* acc, uint32_t n_mats) {
+    for (uint32_t i = threadIdx.x; i < 6u * n_mats; i += blockDim.x) acc[i] = 0.f;
+    __syncthreads();
+}
+
+CRT_D void flush_grad_block(const WaveParams& W, const float* acc) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < 6u * W.n_mats; i += blockDim.x) {
+        const float v = acc[i];
+        if (v == 0.f) continue;
+        const uint32_t m = i / 6u, k = i % 6u;
+        atomicAdd(k < 3u ? W.grad_kd + 3u * m + k : W.grad_ka + 3u * m + (k - 3u), v);
+    }
+}
+
+// The shade_hit hooks of the replay (see NoGrad): w is the adjoint weight of
+// the path's pixel, total the radiance its primal trace returned.
+struct WaveGrad {
+    static constexpr bool kActive = true;
+    float* acc;
+    float3 w, total;
+    CRT_D void emission(uint32_t m, float3 d) { warp_add_grad(acc, m, 3, w * d); }
+    CRT_D void albedo(uint32_t m, float3 kd, float3 color) {
+        const float3 rest = total - color;
+        const float3 g = f3(kd.x != 0.f ? w.x * rest.x / kd.x : 0.f, kd.y != 0.f ? w.y * rest.y / kd.y : 0.f,
+                            kd.z != 0.f ? w.z * rest.z / kd.z : 0.f);
+        warp_add_grad(acc, m, 0, g);
+    }
 };
 
 CRT_D uint4 wave_desc(const WaveParams& W) { return W.waves[W.counters[C_WAVE]]; }
 
 CRT_D void store_state(const WaveParams& W, uint32_t i, const PathState& ps, const Ray& ray, uint32_t pixel,
-                       uint32_t sample) {
+                       uint32_t sample, uint32_t view) {
     W.st_o[i] = make_float4(ray.o.x, ray.o.y, ray.o.z, __uint_as_float(pixel));
     W.st_d[i] = make_float4(ray.d.x, ray.d.y, ray.d.z, __uint_as_float(sample));
     W.st_c[i] = make_float4(ps.color.x, ps.color.y, ps.color.z, __uint_as_float(ps.rng.n));
-    W.st_m[i] = make_float4(ps.mask.x, ps.mask.y, ps.mask.z, __uint_as_float((uint32_t)ps.prev | (ps.bounce << 8)));
+    const uint32_t word = (uint32_t)ps.prev | (ps.bounce << kBounceShift) | (view << kViewShift);
+    W.st_m[i] = make_float4(ps.mask.x, ps.mask.y, ps.mask.z, __uint_as_float(word));
+}
+
+// The segment of a wave holding entry i: the last of segs[0, n) whose
+// start (slot0, or pix0 when by_pixel) is <= i.
+CRT_D uint32_t find_segment(const WaveSeg* segs, uint32_t n, uint32_t i, bool by_pixel) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t start = by_pixel ? segs[mid].pix0 : segs[mid].slot0;
+        if (start <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
 // Warp-aggregated append: returns the slot for this lane (if `want`).
@@ -87,16 +182,27 @@ CRT_D uint32_t warp_append(uint32_t* counter, bool want) {
     return base + __popc(ballot & ((1u << lane) - 1u));
 }
 
+// REPLAY: the adjoint's second trace; each slot first keeps the radiance its
+// primal trace left in st_c and picks up its pixel's adjoint weight.
+template <bool REPLAY>
 __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
     const uint4 wd = wave_desc(W);
-    const uint32_t np = wd.y - wd.x, n = np * (wd.w - wd.z);
+    const WaveSeg* segs = W.segs + wd.x;
+    const uint32_t n = wd.z;
     const uint32_t cur = W.counters[C_CUR];
     for (uint32_t i = blockIdx.x * kWaveBlock + threadIdx.x; i < n; i += gridDim.x * kWaveBlock) {
-        const uint32_t pixel = wd.x + i % np, sample = wd.z + i / np;
+        const WaveSeg sg = segs[find_segment(segs, wd.y, i, false)];
+        const uint32_t np = sg.p1 - sg.p0, k = i - sg.slot0;
+        const uint32_t pixel = sg.p0 + k % np, sample = sg.s0 + k / np;
+        const DevView& V = W.views[sg.view];
+        if (REPLAY) {
+            W.st_L[i] = W.st_c[i];
+            W.st_W[i] = W.adj[V.pix_off + pixel];
+        }
         PathState ps;
         Ray ray;
-        begin_path(W.R, pixel % W.R.width, pixel / W.R.width, pixel, sample, ps, ray);
-        store_state(W, i, ps, ray, pixel, sample);
+        begin_path(V.cam, W.R.seed, V.view_id, pixel % V.width, pixel / V.width, pixel, sample, ps, ray);
+        store_state(W, i, ps, ray, pixel, sample, sg.view);
         W.queue[cur][i] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -115,7 +221,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
 // start(i) (initialise the lane's traversal for queue entry i), step() and
 // finish().
 template <bool REFILL, class Job>
-CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, Job& job) {
+CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, uint32_t chunk, Job& job) {
     if (REFILL) {
         bool active = false;
         WarpPool pool;
@@ -133,14 +239,16 @@ CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, Job& job) {
             }
         }
     } else {
+        // each warp claims `chunk` entries (a multiple of 32) per atomic
         const uint32_t lane = threadIdx.x & 31u;
         for (;;) {
             uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(fetch, 32u);
+            if (lane == 0) base = atomicAdd(fetch, chunk);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
-            if (base + lane < n) {
-                job.start(base + lane);
+            const uint32_t end = min(base + chunk, n);
+            for (uint32_t i = base + lane; i < end; i += 32u) {
+                job.start(i);
                 while (!job.step()) {
                 }
                 job.finish();
@@ -170,18 +278,22 @@ struct ExtendJob {
 };
 
 template <bool REFILL, bool WHOLE_LEAF, bool F32>
-__global__ void __launch_bounds__(kWaveBlock) wf_extend(WaveParams W) {
-    __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
+__global__ void __launch_bounds__(kTraversalBlockMax) wf_extend(WaveParams W) {
+    extern __shared__ uint2 stack_dyn[];
     Stack st;
-    st.sh = stack_sh + threadIdx.x;
-    st.stride = kWaveBlock;
+    st.setup(stack_dyn, blockDim.x, W.stack_depth);
     const uint32_t cur = W.counters[C_CUR];
     ExtendJob<WHOLE_LEAF, F32> job(W, W.queue[cur], st);
-    persistent_loop<REFILL>(W.counters[cur], &W.counters[C_FETCH_EXT], job);
+    persistent_loop<REFILL>(W.counters[cur], &W.counters[C_FETCH_EXT], W.queue_chunk, job);
     count_rays(W.R.ray_counts, job.rays, 0);
 }
 
+// ADJ: the adjoint replay; the same bounce with gradient hooks, shared
+// memory [n_mats][6] floats.
+template <bool ADJ>
 __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
+    extern __shared__ float grad_sh[];
+    if (ADJ) zero_grad_block(grad_sh, W.n_mats);
     const uint32_t cur = W.counters[C_CUR];
     const uint32_t n = W.counters[cur];
     const uint32_t* q = W.queue[cur];
@@ -198,12 +310,13 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
             const float4 hv = W.hit[path];
             const uint32_t pixel = __float_as_uint(o.w), sample = __float_as_uint(d.w);
             const uint32_t pb = __float_as_uint(m.w);
+            const uint32_t view = pb >> kViewShift;
             PathState ps;
             ps.color = xyz(c);
             ps.mask = xyz(m);
             ps.prev = (int)(pb & 0xFFu);
-            ps.bounce = pb >> 8;
-            ps.rng.init(W.R.seed, W.R.view, pixel, sample, __float_as_uint(c.w));
+            ps.bounce = (pb >> kBounceShift) & ((1u << (kViewShift - kBounceShift)) - 1u);
+            ps.rng.init(W.R.seed, W.views[view].view_id, pixel, sample, __float_as_uint(c.w));
             Ray ray;
             ray.o = xyz(o);
             ray.d = xyz(d);
@@ -214,11 +327,15 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
             h.v = hv.w;
             if (h.face < 0) {
                 shade_miss(ps);
+            } else if (ADJ) {
+                WaveGrad g{grad_sh, xyz(W.st_W[path]), xyz(W.st_L[path])};
+                alive = shade_hit(W.R, ps, ray, h, sr, &g) && ps.bounce < W.R.max_depth;
+                want_shadow = sr.valid;
             } else {
                 alive = shade_hit(W.R, ps, ray, h, sr) && ps.bounce < W.R.max_depth;
                 want_shadow = sr.valid;
             }
-            store_state(W, path, ps, ray, pixel, sample);
+            store_state(W, path, ps, ray, pixel, sample, view);
         }
         const uint32_t slot = warp_append(&W.counters[cur ^ 1u], alive);
         if (alive) qn[slot] = path;
@@ -228,18 +345,24 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
             e[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, __uint_as_float(path));
             e[1] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.t_light);
             e[2] = make_float4(sr.contrib.x, sr.contrib.y, sr.contrib.z, __uint_as_float(sr.light_face));
+            if (ADJ) {
+                const float3 w = xyz(W.st_W[path]) * sr.dcontrib;
+                W.shd_grad[ss] = make_float4(w.x, w.y, w.z, __uint_as_float(sr.light_mat));
+            }
         }
     }
+    if (ADJ) flush_grad_block(W, grad_sh);
 }
 
-template <bool WHOLE_LEAF, bool F32>
+template <bool WHOLE_LEAF, bool F32, bool ADJ = false>
 struct ShadowJob {
     const WaveParams& W;
     Stack& st;
+    float* grad;        // ADJ: the block's gradient sums
     Traversal<true, false, WHOLE_LEAF, F32> T;
     uint32_t entry = 0, rays = 0;
 
-    CRT_D ShadowJob(const WaveParams& W_, Stack& st_) : W(W_), st(st_) {}
+    CRT_D ShadowJob(const WaveParams& W_, Stack& st_, float* grad_ = nullptr) : W(W_), st(st_), grad(grad_) {}
     CRT_D void start(uint32_t i) {
         entry = i;
         const float4* e = W.shadow + 3ull * i;
@@ -259,17 +382,36 @@ struct ShadowJob {
         col.y = col.y + c.y;
         col.z = col.z + c.z;
         W.st_c[path] = col;
+        if (ADJ) {
+            const float4 g = W.shd_grad[entry];
+            warp_add_grad(grad, __float_as_uint(g.w), 3, xyz(g));
+        }
     }
 };
 
-template <bool REFILL, bool WHOLE_LEAF, bool F32>
-__global__ void __launch_bounds__(kWaveBlock) wf_shadow(WaveParams W) {
-    __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
+// The adjoint replay's shadow rays (batch fetch, whole leaves): as wf_shadow,
+// and a visible light adds d objective / d (light material ka).  Dynamic
+// shared memory: the traversal stacks, then [n_mats][6] gradient floats.
+template <bool F32>
+__global__ void __launch_bounds__(kTraversalBlockMax) wf_shadow_adj(WaveParams W) {
+    extern __shared__ uint2 stack_dyn[];
+    float* grad = reinterpret_cast<float*>(stack_dyn + (size_t)blockDim.x * W.stack_depth);
+    zero_grad_block(grad, W.n_mats);
     Stack st;
-    st.sh = stack_sh + threadIdx.x;
-    st.stride = kWaveBlock;
+    st.setup(stack_dyn, blockDim.x, W.stack_depth);
+    ShadowJob<true, F32, true> job(W, st, grad);
+    persistent_loop<false>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], W.queue_chunk, job);
+    count_rays(W.R.ray_counts, 0, job.rays);
+    flush_grad_block(W, grad);
+}
+
+template <bool REFILL, bool WHOLE_LEAF, bool F32>
+__global__ void __launch_bounds__(kTraversalBlockMax) wf_shadow(WaveParams W) {
+    extern __shared__ uint2 stack_dyn[];
+    Stack st;
+    st.setup(stack_dyn, blockDim.x, W.stack_depth);
     ShadowJob<WHOLE_LEAF, F32> job(W, st);
-    persistent_loop<REFILL>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], job);
+    persistent_loop<REFILL>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], W.queue_chunk, job);
     count_rays(W.R.ray_counts, 0, job.rays);
 }
 
@@ -310,16 +452,19 @@ __global__ void wf_flip(WaveParams W) {
 
 __global__ void __launch_bounds__(256) wf_accumulate(WaveParams W) {
     const uint4 wd = wave_desc(W);
-    const uint32_t np = wd.y - wd.x, ns = wd.w - wd.z;
-    for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < np; i += gridDim.x * 256) {
-        float4 acc = W.R.accum[wd.x + i];
+    const WaveSeg* segs = W.segs + wd.x;
+    for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < wd.w; i += gridDim.x * 256) {
+        const WaveSeg sg = segs[find_segment(segs, wd.y, i, true)];
+        const uint32_t np = sg.p1 - sg.p0, ns = sg.s1 - sg.s0, k = i - sg.pix0;
+        float4* a = W.R.accum + W.views[sg.view].pix_off + sg.p0 + k;
+        float4 acc = *a;
         for (uint32_t s = 0; s < ns; ++s) {
-            const float4 c = W.st_c[s * np + i];
+            const float4 c = W.st_c[sg.slot0 + s * np + k];
             acc.x = acc.x + c.x;
             acc.y = acc.y + c.y;
             acc.z = acc.z + c.z;
         }
-        W.R.accum[wd.x + i] = acc;
+        *a = acc;
     }
 }
 
@@ -345,8 +490,7 @@ template <bool F32>
 __global__ void __launch_bounds__(kWaveBlock) wf_extend_count(WaveParams W) {
     __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
     Stack st;
-    st.sh = stack_sh + threadIdx.x;
-    st.stride = kWaveBlock;
+    st.setup(stack_sh, kWaveBlock, kStackShared);
     const uint32_t cur = W.counters[C_CUR];
     const uint32_t n = W.counters[cur];
     const uint32_t lane = threadIdx.x & 31u;
@@ -375,8 +519,7 @@ template <bool F32>
 __global__ void __launch_bounds__(kWaveBlock) wf_shadow_count(WaveParams W) {
     __shared__ uint2 stack_sh[kStackShared * kWaveBlock];
     Stack st;
-    st.sh = stack_sh + threadIdx.x;
-    st.stride = kWaveBlock;
+    st.setup(stack_sh, kWaveBlock, kStackShared);
     const uint32_t n = W.counters[C_SHADOW];
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t rays = 0;
@@ -424,10 +567,39 @@ struct WaveGraph {
 
 namespace crt {
 
-static int ensure_wave_buffers(crt_render r) {
-    WaveBuffers& B = r->wave;
-    uint32_t cap = r->opts.wave_paths ? r->opts.wave_paths : kDefaultCapacity;
-    if (B.capacity == cap) return CRT_OK;
+static void drop_set_graphs(WaveSet& s) {
+    delete static_cast<WaveGraph*>(s.graph);
+    delete static_cast<WaveGraph*>(s.adj_graph);
+    s.graph = s.adj_graph = nullptr;
+}
+
+static void destroy_set(WaveSet& s) {
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    drop_set_graphs(s);
+    if (s.acc_done) cudaEventDestroy(s.acc_done);
+    if (s.stream) cudaStreamDestroy(s.stream);
+    s.acc_done = nullptr;
+    s.stream = nullptr;
+}
+
+void destroy_wave_sets(crt_render r) {
+    for (WaveSet& s : r->sets) destroy_set(s);
+    r->sets.clear();
+    if (r->pass_start) cudaEventDestroy(r->pass_start);
+    r->pass_start = nullptr;
+}
+
+// Captured launches hold the camera, stream-independent buffers and
+// options of the moment; they are re-captured on the next pass.
+void drop_wave_graphs(crt_render r) {
+    for (WaveSet& s : r->sets) {
+        if (s.stream) cudaStreamSynchronize(s.stream);
+        drop_set_graphs(s);
+    }
+}
+
+static int alloc_set(WaveSet& S, uint32_t cap) {
+    WaveBuffers& B = S.buf;
     B.capacity = cap;
     const size_t c = cap;
     CRT_CUDA(B.ray_o.alloc(c * 16));
@@ -439,18 +611,53 @@ static int ensure_wave_buffers(crt_render r) {
     CRT_CUDA(B.queue_b.alloc(c * 4));
     CRT_CUDA(B.shadow.alloc(c * 48));
     CRT_CUDA(B.counters.alloc(C_COUNT * 4));
-    CRT_CUDA(cudaMemsetAsync(B.counters.p, 0, C_COUNT * 4, r->stream));
+    CRT_CUDA(cudaMemset(B.counters.p, 0, C_COUNT * 4));
     CRT_CUDA(B.waves.alloc(kMaxWaves * sizeof(uint4)));
+    B.seg_capacity = kMaxWaves;
+    CRT_CUDA(B.segs.alloc((size_t)B.seg_capacity * sizeof(WaveSeg)));
     CRT_CUDA(B.prof.alloc(P_COUNT * sizeof(unsigned long long)));
-    destroy_wave_graph(r->wave_graph);   // captured launches hold the old buffers
-    r->wave_graph = nullptr;
+    CRT_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    CRT_CUDA(cudaEventCreateWithFlags(&S.acc_done, cudaEventDisableTiming));
     return CRT_OK;
 }
 
-static WaveParams wave_params(crt_render r) {
-    WaveBuffers& B = r->wave;
-    WaveParams W;
-    W.R = make_params(r, 0, 0);
+// `count` wave sets of the handle's capacity (reallocated when either changes).
+static int ensure_wave_sets(crt_render r, uint32_t count) {
+    const uint32_t cap = r->opts.wave_paths ? r->opts.wave_paths : kDefaultCapacity;
+    if (r->sets.size() == count && r->sets[0].buf.capacity == cap) return CRT_OK;
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    destroy_wave_sets(r);
+    CRT_CUDA(cudaEventCreateWithFlags(&r->pass_start, cudaEventDisableTiming));
+    r->sets.resize(count);
+    for (WaveSet& s : r->sets) {
+        int st = alloc_set(s, cap);
+        if (st != CRT_OK) {
+            destroy_wave_sets(r);
+            return st;
+        }
+    }
+    return CRT_OK;
+}
+
+// Room for n segments in a set's table; a larger table invalidates the
+// set's captured graph, which holds the old address.
+static int ensure_segments(WaveSet& set, size_t n) {
+    WaveBuffers& B = set.buf;
+    if (n <= B.seg_capacity) return CRT_OK;
+    if (n > (size_t)UINT32_MAX) return set_error(CRT_ERR_LIMIT, "too many wave segments");
+    CRT_CUDA(cudaStreamSynchronize(set.stream));
+    drop_set_graphs(set);
+    B.seg_capacity = (uint32_t)std::max<size_t>(n, 2ull * B.seg_capacity);
+    CRT_CUDA(B.segs.alloc((size_t)B.seg_capacity * sizeof(WaveSeg)));
+    return CRT_OK;
+}
+
+static WaveParams wave_params(crt_render r, WaveSet& set) {
+    WaveBuffers& B = set.buf;
+    WaveParams W{};
+    W.R = make_params(r, 0, 0, 0);
+    W.R.accum = r->accum.as<float4>();   // every view; segments add their offsets
+    W.views = r->view_table.as<DevView>();
     W.st_o = B.ray_o.as<float4>();
     W.st_d = B.ray_d.as<float4>();
     W.st_c = B.color.as<float4>();
@@ -461,120 +668,377 @@ static WaveParams wave_params(crt_render r) {
     W.shadow = B.shadow.as<float4>();
     W.counters = B.counters.as<uint32_t>();
     W.waves = B.waves.as<uint4>();
+    W.segs = B.segs.as<WaveSeg>();
     W.prof = B.prof.as<unsigned long long>();
+    W.stack_depth = (int)traversal_stack(r->opts);
+    W.queue_chunk = queue_chunk(r->opts);
     return W;
 }
 
 struct WaveGrids {
-    int gen, ext, shd, acc;
+    int gen, ext, shd, acc, cnt;
+    int tblock;          // extend / shadow threads per block
+    size_t tsmem;        // their dynamic shared memory (traversal stacks)
     WaveKernel extend, shadow, extend_count, shadow_count;
 };
 
-// Kernel choice and grid sizes, queried before a capture starts.
-static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32) {
+// Kernel choice and launch shapes, queried before a capture starts.
+static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32, uint32_t block, uint32_t depth) {
     WaveGrids g;
     g.extend = extend_kernel(flags, f32);
     g.shadow = shadow_kernel(flags, f32);
     g.extend_count = f32 ? wf_extend_count<true> : wf_extend_count<false>;
     g.shadow_count = f32 ? wf_shadow_count<true> : wf_shadow_count<false>;
+    g.tblock = (int)block;
+    g.tsmem = (size_t)block * depth * sizeof(uint2);
+    cudaFuncSetAttribute((const void*)g.extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.tsmem);
+    cudaFuncSetAttribute((const void*)g.shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.tsmem);
     g.gen = grid_for(capacity, kWaveBlock, 16);
-    g.ext = persistent_grid((const void*)g.extend, kWaveBlock, 0);
-    g.shd = persistent_grid((const void*)g.shadow, kWaveBlock, 0);
+    g.ext = persistent_grid((const void*)g.extend, g.tblock, g.tsmem);
+    g.shd = persistent_grid((const void*)g.shadow, g.tblock, g.tsmem);
+    g.cnt = persistent_grid((const void*)g.extend_count, kWaveBlock, 0);
     g.acc = grid_for(capacity, 256, 8);
     return g;
 }
 
-// Enqueue one wave; captured into the handle's graph.
-static void enqueue_wave(const WaveParams& W, const WaveGrids& G, uint32_t max_depth, cudaStream_t s) {
-    wf_generate<<<G.gen, kWaveBlock, 0, s>>>(W);
+static WaveGrids wave_grids(crt_render r, uint32_t capacity) {
+    return wave_grids(capacity, r->opts.flags, uses_f32_nodes(r), traversal_block(r->opts), traversal_stack(r->opts));
+}
+
+// Enqueue the body of one wave (generation and every bounce); captured into
+// a wave set's graph.  The accumulate and wave-advance kernels follow it
+// outside the graph so that accumulates of concurrent sets can be ordered.
+static void enqueue_wave_body(const WaveParams& W, const WaveGrids& G, uint32_t max_depth, cudaStream_t s) {
+    wf_generate<false><<<G.gen, kWaveBlock, 0, s>>>(W);
     for (uint32_t b = 0; b < max_depth; ++b) {
-        G.extend<<<G.ext, kWaveBlock, 0, s>>>(W);
-        wf_shade<<<G.gen, kWaveBlock, 0, s>>>(W);
-        G.shadow<<<G.shd, kWaveBlock, 0, s>>>(W);
+        G.extend<<<G.ext, G.tblock, G.tsmem, s>>>(W);
+        wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
+        G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W);
         wf_flip<<<1, 1, 0, s>>>(W);
     }
-    wf_accumulate<<<G.acc, 256, 0, s>>>(W);
-    wf_next_wave<<<1, 1, 0, s>>>(W);
 }
 
-// Wave descriptors: whole sample layers when the image fits, else pixel
-// ranges of one sample each.
-static std::vector<uint4> make_waves(uint32_t npix, uint32_t capacity, uint32_t spp0, uint32_t nspp) {
+// The waves of a pass, as descriptors {first segment, segments, paths,
+// accumulate entries} over one segment list.
+struct WavePlan {
     std::vector<uint4> waves;
-    if (npix <= capacity) {
-        const uint32_t layers = capacity / npix;
-        for (uint32_t s = 0; s < nspp; s += layers)
-            waves.push_back(make_uint4(0, npix, spp0 + s, spp0 + std::min(nspp, s + layers)));
-    } else {
-        for (uint32_t s = 0; s < nspp; ++s)
-            for (uint32_t p = 0; p < npix; p += capacity)
-                waves.push_back(make_uint4(p, std::min(npix, p + capacity), spp0 + s, spp0 + s + 1));
-    }
-    return waves;
-}
+    std::vector<WaveSeg> segs;
+};
 
-// Uploads one chunk of descriptors and restarts C_CUR / C_WAVE at zero.
-static int upload_waves(crt_render r, const std::vector<uint4>& waves, size_t w0, size_t nw) {
-    WaveBuffers& B = r->wave;
-    const uint32_t zero[2] = {0, 0};
-    CRT_CUDA(cudaMemcpyAsync(B.waves.p, waves.data() + w0, nw * sizeof(uint4), cudaMemcpyHostToDevice,
-                             r->stream));
-    CRT_CUDA(cudaMemcpyAsync(B.counters.as<uint32_t>() + C_CUR, zero, 8, cudaMemcpyHostToDevice, r->stream));
-    return CRT_OK;
-}
-
-int wavefront_pass(crt_render r, uint32_t spp0, uint32_t nspp) {
-    int st = ensure_wave_buffers(r);
-    if (st != CRT_OK) return st;
-    WaveBuffers& B = r->wave;
-    const std::vector<uint4> waves = make_waves(r->width * r->height, B.capacity, spp0, nspp);
-    // The wave's launch sequence is captured once per handle and replayed.
-    WaveGraph* g = static_cast<WaveGraph*>(r->wave_graph);
-    if (!g) {
-        g = new WaveGraph();
-        r->wave_graph = g;
-        const WaveParams W = wave_params(r);
-        const WaveGrids G = wave_grids(B.capacity, r->opts.flags, r->scene->dev.fnodes != nullptr);
-        CRT_CUDA(cudaGetLastError());
-        // Captured on a private stream: the caller's stream may be the legacy
-        // default stream, which cannot be captured.  The graph is launched on
-        // the caller's stream below.
-        cudaStream_t cap = nullptr;
-        CRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            enqueue_wave(W, G, r->opts.max_depth, cap);
-            e = cudaStreamEndCapture(cap, &g->graph);
+// Packs every view's work into waves of at most `capacity` paths.  Views are
+// taken in order; each view adds at most one segment to a wave -- whole
+// sample layers when the rest of its image fits, else a pixel range of one
+// sample -- so no pixel appears twice in a wave, and each pixel's samples
+// arrive in sample order wave after wave.  A lone view packs exactly like the
+// single-image rule: whole layers while the image fits, else pixel ranges.
+static WavePlan make_waves(const crt_render_s* r, const std::vector<ViewWork>& work, uint32_t capacity) {
+    struct Pending {
+        uint32_t view, npix, s, end, p;   // next sample s (of [s, end)), next pixel p of that sample
+    };
+    std::vector<Pending> pend;
+    for (uint32_t v = 0; v < (uint32_t)work.size(); ++v)
+        if (work[v].nspp)
+            pend.push_back({v, r->views[v].npix(), work[v].spp0, work[v].spp0 + work[v].nspp, 0});
+    WavePlan plan;
+    size_t first = 0;   // first view with work left
+    while (first < pend.size()) {
+        const uint32_t seg0 = (uint32_t)plan.segs.size();
+        uint32_t used = 0, pixels = 0;
+        for (size_t j = first; j < pend.size() && used < capacity; ++j) {
+            Pending& P = pend[j];
+            if (P.s >= P.end) continue;
+            const uint32_t room = capacity - used;
+            WaveSeg g{};
+            g.view = P.view;
+            g.slot0 = used;
+            g.pix0 = pixels;
+            if (P.p == 0 && P.npix <= room) {
+                const uint32_t k = std::min(room / P.npix, P.end - P.s);
+                g.p0 = 0;
+                g.p1 = P.npix;
+                g.s0 = P.s;
+                g.s1 = P.s + k;
+                used += k * P.npix;
+                P.s += k;
+            } else {
+                const uint32_t take = std::min(P.npix - P.p, room);
+                g.p0 = P.p;
+                g.p1 = P.p + take;
+                g.s0 = P.s;
+                g.s1 = P.s + 1;
+                used += take;
+                P.p += take;
+                if (P.p == P.npix) {
+                    P.p = 0;
+                    P.s += 1;
+                }
+            }
+            pixels += g.p1 - g.p0;
+            plan.segs.push_back(g);
         }
-        cudaStreamDestroy(cap);
-        if (e != cudaSuccess) return cuda_error(e, "capture wave graph");
-        CRT_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));
+        plan.waves.push_back(make_uint4(seg0, (uint32_t)plan.segs.size() - seg0, used, pixels));
+        while (first < pend.size() && pend[first].s >= pend[first].end) ++first;
     }
-    for (size_t w0 = 0; w0 < waves.size(); w0 += kMaxWaves) {
-        const size_t nw = std::min<size_t>(kMaxWaves, waves.size() - w0);
-        if ((st = upload_waves(r, waves, w0, nw)) != CRT_OK) return st;
-        for (size_t w = 0; w < nw; ++w) CRT_CUDA(cudaGraphLaunch(g->exec, r->stream));
+    return plan;
+}
+
+// Waves [w0, w1) of a plan, taking every `stride`-th one, with their
+// segments rebased to a table of their own.
+static void slice_waves(const WavePlan& plan, size_t w0, size_t w1, size_t stride, std::vector<uint4>& waves,
+                        std::vector<WaveSeg>& segs) {
+    waves.clear();
+    segs.clear();
+    for (size_t w = w0; w < w1; w += stride) {
+        uint4 d = plan.waves[w];
+        const uint32_t base = (uint32_t)segs.size();
+        segs.insert(segs.end(), plan.segs.begin() + d.x, plan.segs.begin() + d.x + d.y);
+        d.x = base;
+        waves.push_back(d);
+    }
+}
+
+// Uploads a set's descriptors (at most kMaxWaves) and segments on `s` and
+// restarts its C_CUR / C_WAVE at zero.
+static int upload_waves(WaveSet& set, const std::vector<uint4>& waves, const std::vector<WaveSeg>& segs,
+                        cudaStream_t s) {
+    WaveBuffers& B = set.buf;
+    const uint32_t zero[2] = {0, 0};
+    CRT_CUDA(cudaMemcpyAsync(B.waves.p, waves.data(), waves.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
+    CRT_CUDA(cudaMemcpyAsync(B.segs.p, segs.data(), segs.size() * sizeof(WaveSeg), cudaMemcpyHostToDevice, s));
+    CRT_CUDA(cudaMemcpyAsync(B.counters.as<uint32_t>() + C_CUR, zero, 8, cudaMemcpyHostToDevice, s));
+    return CRT_OK;
+}
+
+static int capture_set_graph(crt_render r, WaveSet& set) {
+    if (set.graph) return CRT_OK;
+    WaveGraph* g = new WaveGraph();
+    set.graph = g;
+    const WaveParams W = wave_params(r, set);
+    const WaveGrids G = wave_grids(r, set.buf.capacity);
+    CRT_CUDA(cudaGetLastError());
+    // Captured on a private stream; launched on the set's stream.
+    cudaStream_t cap = nullptr;
+    CRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        enqueue_wave_body(W, G, r->opts.max_depth, cap);
+        e = cudaStreamEndCapture(cap, &g->graph);
+    }
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return cuda_error(e, "capture wave graph");
+    CRT_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));
+    return CRT_OK;
+}
+
+// A pass: wave w runs on set w % K.  Each set's stream replays its graph for
+// the wave body, then waits for the previous wave's accumulate (on whichever
+// set ran it) before accumulating, so every pixel adds its samples in sample
+// order while the bodies of consecutive waves overlap: one wave's thin late
+// bounces share the GPU with the next wave's heavy first bounces.
+int wavefront_pass(crt_render r, const std::vector<ViewWork>& work) {
+    const uint32_t K = r->opts.wave_sets ? r->opts.wave_sets : kDefaultWaveSets;
+    int st = ensure_wave_sets(r, K);
+    if (st != CRT_OK) return st;
+    const uint32_t cap = r->sets[0].buf.capacity;
+    const WavePlan plan = make_waves(r, work, cap);
+    if (r->scene_generation != r->scene->generation) {   // the scene's BVH was rebuilt
+        drop_wave_graphs(r);
+        r->scene_generation = r->scene->generation;
+    }
+    const size_t chunk = (size_t)kMaxWaves * K;
+    std::vector<uint4> mine;
+    std::vector<WaveSeg> segs;
+    // segment tables large enough for every chunk before any graph is captured
+    for (size_t c0 = 0; c0 < plan.waves.size(); c0 += chunk)
+        for (uint32_t k = 0; k < K; ++k) {
+            slice_waves(plan, c0 + k, std::min(plan.waves.size(), c0 + chunk), K, mine, segs);
+            if ((st = ensure_segments(r->sets[k], segs.size())) != CRT_OK) return st;
+        }
+    for (WaveSet& s : r->sets)
+        if ((st = capture_set_graph(r, s)) != CRT_OK) return st;
+    // the sets start after everything already queued on the handle's stream
+    CRT_CUDA(cudaEventRecord(r->pass_start, r->stream));
+    for (WaveSet& s : r->sets) CRT_CUDA(cudaStreamWaitEvent(s.stream, r->pass_start, 0));
+    const WaveGrids G = wave_grids(r, cap);
+    int prev = -1;
+    for (size_t c0 = 0; c0 < plan.waves.size(); c0 += chunk) {
+        const size_t c1 = std::min(plan.waves.size(), c0 + chunk);
+        for (uint32_t k = 0; k < K; ++k) {
+            slice_waves(plan, c0 + k, c1, K, mine, segs);
+            if (!mine.empty() && (st = upload_waves(r->sets[k], mine, segs, r->sets[k].stream))) return st;
+        }
+        for (size_t w = c0; w < c1; ++w) {
+            const int k = (int)(w % K);
+            WaveSet& s = r->sets[k];
+            const WaveParams W = wave_params(r, s);
+            CRT_CUDA(cudaGraphLaunch(static_cast<WaveGraph*>(s.graph)->exec, s.stream));
+            if (prev >= 0) CRT_CUDA(cudaStreamWaitEvent(s.stream, r->sets[prev].acc_done, 0));
+            wf_accumulate<<<G.acc, 256, 0, s.stream>>>(W);
+            wf_next_wave<<<1, 1, 0, s.stream>>>(W);
+            CRT_CUDA(cudaEventRecord(s.acc_done, s.stream));
+            prev = k;
+        }
+    }
+    CRT_CUDA(cudaGetLastError());
+    // the handle's stream continues after every set's last accumulate
+    for (WaveSet& s : r->sets) CRT_CUDA(cudaStreamWaitEvent(r->stream, s.acc_done, 0));
+    return CRT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint pass (crt_render_adjoint): every wave is traced twice from the same
+// Philox counters -- the primal trace leaves each path's radiance in st_c,
+// then the replay re-runs the path and turns each event into gradient terms
+// (WaveGrad) -- so nothing per vertex is stored.
+// ---------------------------------------------------------------------------
+static int ensure_adjoint_buffers(WaveSet& set) {
+    WaveBuffers& B = set.buf;
+    if (B.adj_L.p) return CRT_OK;
+    const size_t c = B.capacity;
+    CRT_CUDA(B.adj_L.alloc(c * 16));
+    CRT_CUDA(B.adj_W.alloc(c * 16));
+    CRT_CUDA(B.adj_shadow.alloc(c * 16));
+    return CRT_OK;
+}
+
+struct AdjointGrids {
+    int shd;
+    size_t shade_smem, shadow_smem;
+    WaveKernel shadow;
+};
+
+static AdjointGrids adjoint_grids(crt_render r, const WaveGrids& G) {
+    AdjointGrids a;
+    const size_t gsm = (size_t)6 * r->scene->n_mats * sizeof(float);
+    a.shade_smem = gsm;
+    a.shadow_smem = G.tsmem + gsm;
+    a.shadow = uses_f32_nodes(r) ? wf_shadow_adj<true> : wf_shadow_adj<false>;
+    cudaFuncSetAttribute((const void*)a.shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shadow_smem);
+    cudaFuncSetAttribute((const void*)wf_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)a.shade_smem);
+    a.shd = persistent_grid((const void*)a.shadow, G.tblock, a.shadow_smem);
+    return a;
+}
+
+static WaveParams adjoint_params(crt_render r, WaveSet& set, const float4* adj, float* gkd, float* gka) {
+    WaveParams W = wave_params(r, set);
+    W.adj = adj;
+    W.st_L = set.buf.adj_L.as<float4>();
+    W.st_W = set.buf.adj_W.as<float4>();
+    W.shd_grad = set.buf.adj_shadow.as<float4>();
+    W.grad_kd = gkd;
+    W.grad_ka = gka;
+    W.n_mats = r->scene->n_mats;
+    return W;
+}
+
+static int capture_adjoint_graph(crt_render r, WaveSet& set, const float4* adj, float* gkd, float* gka) {
+    if (set.adj_graph && set.adj_key[0] == adj && set.adj_key[1] == gkd && set.adj_key[2] == gka) return CRT_OK;
+    delete static_cast<WaveGraph*>(set.adj_graph);
+    WaveGraph* g = new WaveGraph();
+    set.adj_graph = g;
+    set.adj_key[0] = adj;
+    set.adj_key[1] = gkd;
+    set.adj_key[2] = gka;
+    const WaveParams W = adjoint_params(r, set, adj, gkd, gka);
+    const WaveGrids G = wave_grids(r, set.buf.capacity);
+    const AdjointGrids A = adjoint_grids(r, G);
+    CRT_CUDA(cudaGetLastError());
+    cudaStream_t cap = nullptr;
+    CRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        enqueue_wave_body(W, G, r->opts.max_depth, cap);     // primal trace
+        wf_generate<true><<<G.gen, kWaveBlock, 0, cap>>>(W);  // replay
+        for (uint32_t b = 0; b < r->opts.max_depth; ++b) {
+            G.extend<<<G.ext, G.tblock, G.tsmem, cap>>>(W);
+            wf_shade<true><<<G.gen, kWaveBlock, A.shade_smem, cap>>>(W);
+            A.shadow<<<A.shd, G.tblock, A.shadow_smem, cap>>>(W);
+            wf_flip<<<1, 1, 0, cap>>>(W);
+        }
+        e = cudaStreamEndCapture(cap, &g->graph);
+    }
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return cuda_error(e, "capture adjoint graph");
+    CRT_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));
+    return CRT_OK;
+}
+
+// Waves run on the K sets round-robin, concurrently: gradient sums need no
+// ordering (their atomic adds commute up to rounding).
+int wavefront_adjoint(crt_render r, const std::vector<ViewWork>& work, const float4* adj, float* gkd,
+                      float* gka) {
+    if ((size_t)6 * r->scene->n_mats * sizeof(float) > 24u * 1024u)
+        return set_error(CRT_ERR_LIMIT, "the adjoint supports at most 1024 materials");
+    const uint32_t K = r->opts.wave_sets ? r->opts.wave_sets : kDefaultWaveSets;
+    int st = ensure_wave_sets(r, K);
+    if (st != CRT_OK) return st;
+    for (WaveSet& s : r->sets)
+        if ((st = ensure_adjoint_buffers(s)) != CRT_OK) return st;
+    const uint32_t cap = r->sets[0].buf.capacity;
+    const WavePlan plan = make_waves(r, work, cap);
+    if (r->scene_generation != r->scene->generation) {
+        drop_wave_graphs(r);
+        r->scene_generation = r->scene->generation;
+    }
+    const size_t chunk = (size_t)kMaxWaves * K;
+    std::vector<uint4> mine;
+    std::vector<WaveSeg> segs;
+    for (size_t c0 = 0; c0 < plan.waves.size(); c0 += chunk)
+        for (uint32_t k = 0; k < K; ++k) {
+            slice_waves(plan, c0 + k, std::min(plan.waves.size(), c0 + chunk), K, mine, segs);
+            if ((st = ensure_segments(r->sets[k], segs.size())) != CRT_OK) return st;
+        }
+    for (WaveSet& s : r->sets)
+        if ((st = capture_adjoint_graph(r, s, adj, gkd, gka)) != CRT_OK) return st;
+    CRT_CUDA(cudaEventRecord(r->pass_start, r->stream));
+    for (WaveSet& s : r->sets) CRT_CUDA(cudaStreamWaitEvent(s.stream, r->pass_start, 0));
+    for (size_t c0 = 0; c0 < plan.waves.size(); c0 += chunk) {
+        const size_t c1 = std::min(plan.waves.size(), c0 + chunk);
+        for (uint32_t k = 0; k < K; ++k) {
+            slice_waves(plan, c0 + k, c1, K, mine, segs);
+            if (!mine.empty() && (st = upload_waves(r->sets[k], mine, segs, r->sets[k].stream))) return st;
+        }
+        for (size_t w = c0; w < c1; ++w) {
+            WaveSet& s = r->sets[w % K];
+            CRT_CUDA(cudaGraphLaunch(static_cast<WaveGraph*>(s.adj_graph)->exec, s.stream));
+            wf_next_wave<<<1, 1, 0, s.stream>>>(wave_params(r, s));
+        }
+    }
+    CRT_CUDA(cudaGetLastError());
+    for (WaveSet& s : r->sets) {
+        CRT_CUDA(cudaEventRecord(s.acc_done, s.stream));
+        CRT_CUDA(cudaStreamWaitEvent(r->stream, s.acc_done, 0));
     }
     return CRT_OK;
 }
 
-// Same launch sequence as enqueue_wave(), one kernel at a time with CUDA
+// Same launch sequence as a wave graph, one kernel at a time with CUDA
 // events around each launch, plus untimed counting re-runs of each traversal.
-int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage_profile* out) {
-    int st = ensure_wave_buffers(r);
+// The profile pass runs its waves one after another on set 0, on the
+// handle's stream (after any earlier pass has joined it).
+int wavefront_profile_pass(crt_render r, const std::vector<ViewWork>& work, crt_stage_profile* out) {
+    int st = ensure_wave_sets(r, r->opts.wave_sets ? r->opts.wave_sets : kDefaultWaveSets);
     if (st != CRT_OK) return st;
-    WaveBuffers& B = r->wave;
-    const std::vector<uint4> waves = make_waves(r->width * r->height, B.capacity, spp0, nspp);
-    const WaveParams W = wave_params(r);
-    const WaveGrids G = wave_grids(B.capacity, r->opts.flags, r->scene->dev.fnodes != nullptr);
+    WaveSet& set0 = r->sets[0];
+    WaveBuffers& B = set0.buf;
+    const WavePlan plan = make_waves(r, work, B.capacity);
+    std::vector<uint4> mine;
+    std::vector<WaveSeg> segs;
+    for (size_t w0 = 0; w0 < plan.waves.size(); w0 += kMaxWaves) {
+        slice_waves(plan, w0, std::min(plan.waves.size(), w0 + kMaxWaves), 1, mine, segs);
+        if ((st = ensure_segments(set0, segs.size())) != CRT_OK) return st;
+    }
+    const WaveParams W = wave_params(r, set0);
+    const WaveGrids G = wave_grids(r, B.capacity);
     CRT_CUDA(cudaMemsetAsync(B.prof.p, 0, B.prof.bytes, r->stream));
     cudaEvent_t e0, e1;
     CRT_CUDA(cudaEventCreate(&e0));
     CRT_CUDA(cudaEventCreate(&e1));
     cudaStream_t s = r->stream;
     cudaError_t err = cudaSuccess;
-    auto timed = [&](int stage, auto launch) {
-        if (err != cudaSuccess) return;
+    auto timed = [&](int stage, auto launch) -> float {
+        if (err != cudaSuccess) return 0.f;
         cudaEventRecord(e0, s);
         launch();
         cudaEventRecord(e1, s);
@@ -584,20 +1048,30 @@ int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage
         if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
         out->ms[stage] += ms;
         out->launches[stage] += 1;
+        return ms;
     };
-    for (size_t w0 = 0; w0 < waves.size() && err == cudaSuccess; w0 += kMaxWaves) {
-        const size_t nw = std::min<size_t>(kMaxWaves, waves.size() - w0);
-        if ((st = upload_waves(r, waves, w0, nw)) != CRT_OK) break;
-        for (size_t w = 0; w < nw; ++w) {
-            timed(0, [&] { wf_generate<<<G.gen, kWaveBlock, 0, s>>>(W); });
+    // queue lengths (device counters) read after the stage that consumes them
+    auto counter = [&](uint32_t idx) -> uint32_t {
+        uint32_t v = 0;
+        if (err == cudaSuccess) err = cudaMemcpy(&v, B.counters.as<uint32_t>() + idx, 4, cudaMemcpyDeviceToHost);
+        return v;
+    };
+    for (size_t w0 = 0; w0 < plan.waves.size() && err == cudaSuccess; w0 += kMaxWaves) {
+        slice_waves(plan, w0, std::min(plan.waves.size(), w0 + kMaxWaves), 1, mine, segs);
+        if ((st = upload_waves(set0, mine, segs, s)) != CRT_OK) break;
+        for (size_t w = 0; w < mine.size(); ++w) {
+            timed(0, [&] { wf_generate<false><<<G.gen, kWaveBlock, 0, s>>>(W); });
             for (uint32_t b = 0; b < r->opts.max_depth; ++b) {
-                timed(1, [&] { G.extend<<<G.ext, kWaveBlock, 0, s>>>(W); });
+                const uint32_t bb = b < 15 ? b : 15;
+                out->extend_ms_by_bounce[bb] += timed(1, [&] { G.extend<<<G.ext, G.tblock, G.tsmem, s>>>(W); });
+                out->extend_rays_by_bounce[bb] += counter(counter(C_CUR));
                 wf_reset_count_fetch<<<1, 1, 0, s>>>(W);
-                G.extend_count<<<G.ext, kWaveBlock, 0, s>>>(W);
-                timed(2, [&] { wf_shade<<<G.gen, kWaveBlock, 0, s>>>(W); });
-                timed(3, [&] { G.shadow<<<G.shd, kWaveBlock, 0, s>>>(W); });
+                G.extend_count<<<G.cnt, kWaveBlock, 0, s>>>(W);
+                timed(2, [&] { wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W); });
+                out->shadow_ms_by_bounce[bb] += timed(3, [&] { G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W); });
+                out->shadow_rays_by_bounce[bb] += counter(C_SHADOW);
                 wf_reset_count_fetch<<<1, 1, 0, s>>>(W);
-                G.shadow_count<<<G.shd, kWaveBlock, 0, s>>>(W);
+                G.shadow_count<<<G.cnt, kWaveBlock, 0, s>>>(W);
                 timed(5, [&] { wf_flip<<<1, 1, 0, s>>>(W); });
             }
             timed(4, [&] { wf_accumulate<<<G.acc, 256, 0, s>>>(W); });
@@ -620,7 +1094,6 @@ int wavefront_profile_pass(crt_render r, uint32_t spp0, uint32_t nspp, crt_stage
     return CRT_OK;
 }
 
-void destroy_wave_graph(void* g) { delete static_cast<WaveGraph*>(g); }
 
 // ---------------------------------------------------------------------------
 // Allocation-free tile renders (crt_render_tile_noalloc).
@@ -647,10 +1120,14 @@ constexpr size_t kNoAllocOff[] = {
     80ull * kNoAllocPaths,              // queue 0  4 B per path
     84ull * kNoAllocPaths,              // queue 1
     88ull * kNoAllocPaths,              // shadow requests 48 B per path
-    136ull * kNoAllocPaths,             // counters (C_COUNT words), then the wave descriptor
-    136ull * kNoAllocPaths + 256,       // ray counts (2 x u64)
+    136ull * kNoAllocPaths,             // counters (C_COUNT words)
+    136ull * kNoAllocPaths + 64,        // wave descriptor (uint4)
+    136ull * kNoAllocPaths + 96,        // its one segment (WaveSeg)
+    136ull * kNoAllocPaths + 128,       // ray counts (2 x u64)
+    136ull * kNoAllocPaths + 256,       // the view (DevView)
 };
 constexpr size_t kNoAllocBytes = 136ull * kNoAllocPaths + 512;
+static_assert(sizeof(WaveSeg) == 32 && sizeof(DevView) <= 256, "no-alloc scratch layout");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -674,13 +1151,15 @@ static int noalloc_scratch(void** out) {
     return CRT_OK;
 }
 
-// Starts a call: clears the counters and ray counts and installs the wave
-// descriptor (everything that must start at zero; path state is always
-// written before it is read).
-__global__ void wf_noalloc_begin(WaveParams W, uint4 wave) {
+// Starts a call: clears the counters and ray counts (everything that must
+// start at zero; path state is always written before it is read) and
+// installs the view, the wave's one segment and its descriptor.
+__global__ void wf_noalloc_begin(WaveParams W, uint4 wave, WaveSeg seg, DevView view) {
     for (int i = 0; i < C_COUNT; ++i) W.counters[i] = 0;
     W.R.ray_counts[0] = W.R.ray_counts[1] = 0;
     const_cast<uint4*>(W.waves)[0] = wave;
+    const_cast<WaveSeg*>(W.segs)[0] = seg;
+    const_cast<DevView*>(W.views)[0] = view;
 }
 
 }  // namespace crt
@@ -705,14 +1184,15 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     crt_render_options o;
     if (opts) o = *opts;
     else crt_render_options_default(&o);
-    if (o.max_depth == 0 || o.max_depth > 1024) return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
+    if (int st = check_render_options(o)) return st;
     void* base = nullptr;
     int st = noalloc_scratch(&base);
     if (st != CRT_OK) return st;
     unsigned char* b = static_cast<unsigned char*>(base);
-    WaveParams W;
+    WaveParams W{};
     RenderParams& R = W.R;
-    R.S = scene->dev;
+    const bool f32 = uses_f32_nodes(scene, o.node_format);
+    R.S = scene->view(f32);
     R.cam = to_device_camera(*camera);
     R.accum = reinterpret_cast<float4*>(d_accum);
     R.width = width;
@@ -722,7 +1202,9 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     R.spp0 = spp0;
     R.nspp = nspp;
     R.max_depth = o.max_depth;
-    R.ray_counts = reinterpret_cast<unsigned long long*>(b + kNoAllocOff[9]);
+    R.ka_scale = 3.0f * scene->dev.lights_area;
+    R.ray_counts = reinterpret_cast<unsigned long long*>(b + kNoAllocOff[11]);
+    W.views = reinterpret_cast<const DevView*>(b + kNoAllocOff[12]);
     W.st_o = reinterpret_cast<float4*>(b + kNoAllocOff[0]);
     W.st_d = reinterpret_cast<float4*>(b + kNoAllocOff[1]);
     W.st_c = reinterpret_cast<float4*>(b + kNoAllocOff[2]);
@@ -732,16 +1214,26 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     W.queue[1] = reinterpret_cast<uint32_t*>(b + kNoAllocOff[6]);
     W.shadow = reinterpret_cast<float4*>(b + kNoAllocOff[7]);
     W.counters = reinterpret_cast<uint32_t*>(b + kNoAllocOff[8]);
-    W.waves = reinterpret_cast<const uint4*>(b + kNoAllocOff[8] + 64);
+    W.waves = reinterpret_cast<const uint4*>(b + kNoAllocOff[9]);
+    W.segs = reinterpret_cast<const WaveSeg*>(b + kNoAllocOff[10]);
     W.prof = nullptr;
-    const WaveGrids G = wave_grids(kNoAllocPaths, o.flags, scene->dev.fnodes != nullptr);
+    W.stack_depth = (int)traversal_stack(o);
+    W.queue_chunk = queue_chunk(o);
+    const WaveGrids G = wave_grids(kNoAllocPaths, o.flags, f32, traversal_block(o), W.stack_depth);
     cudaStream_t s = (cudaStream_t)stream;
-    wf_noalloc_begin<<<1, 1, 0, s>>>(W, make_uint4(pixel0, pixel0 + pixel_count, spp0, spp0 + nspp));
-    wf_generate<<<G.gen, kWaveBlock, 0, s>>>(W);
+    DevView view;
+    view.cam = R.cam;
+    view.width = width;
+    view.height = height;
+    view.view_id = o.view_id;
+    view.pix_off = 0;
+    const WaveSeg seg{0, pixel0, pixel0 + pixel_count, spp0, spp0 + nspp, 0, 0, 0};
+    wf_noalloc_begin<<<1, 1, 0, s>>>(W, make_uint4(0, 1, pixel_count * nspp, pixel_count), seg, view);
+    wf_generate<false><<<G.gen, kWaveBlock, 0, s>>>(W);
     for (uint32_t k = 0; k < o.max_depth; ++k) {
-        G.extend<<<G.ext, kWaveBlock, 0, s>>>(W);
-        wf_shade<<<G.gen, kWaveBlock, 0, s>>>(W);
-        G.shadow<<<G.shd, kWaveBlock, 0, s>>>(W);
+        G.extend<<<G.ext, G.tblock, G.tsmem, s>>>(W);
+        wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
+        G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W);
         wf_flip<<<1, 1, 0, s>>>(W);
     }
     wf_accumulate<<<G.acc, 256, 0, s>>>(W);

@@ -15,7 +15,8 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from ._lib import Camera, Material, RenderOptions, SceneDesc, SceneInfo, check, load
+from ._lib import (Camera, Material, RenderOptions, SceneDesc, SceneInfo, TuneParams, TuneResult,
+                   View, check, load)
 from .scenes import NO_TEXTURE, SceneArrays, texture_texels
 
 NODE_DT = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base", "<u4"),
@@ -40,24 +41,29 @@ def camera_from_json(spec, width: int, height: int) -> Camera:
     return cam
 
 
-def bvh_build_host(positions: np.ndarray):
-    """Host-only 8-wide BVH build: (nodes, triangle records, max depth)."""
+def bvh_build_host(positions: np.ndarray, width: int = 8):
+    """Host-only BVH build (4 or 8 children per node): (nodes, triangle
+    records, max depth)."""
     pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
     n = len(pos)
     nn, depth = C.c_uint32(0), C.c_uint32(0)
     L = load()
-    check(L.crt_bvh_build_host(_ptr(pos), n, C.byref(nn), C.byref(depth), None, None))
+    check(L.crt_bvh_build_host(_ptr(pos), n, width, C.byref(nn), C.byref(depth), None, None))
     nodes = np.zeros(nn.value, NODE_DT)
     tris = np.zeros(n, TRI_DT)
-    check(L.crt_bvh_build_host(_ptr(pos), n, C.byref(nn), C.byref(depth), _ptr(nodes), _ptr(tris)))
+    check(L.crt_bvh_build_host(_ptr(pos), n, width, C.byref(nn), C.byref(depth), _ptr(nodes),
+                               _ptr(tris)))
     return nodes, tris, depth.value
+
+
+NODE_FORMATS = {"q8": _lib.NODES_Q8, "f32": _lib.NODES_F32}
 
 
 class GB300Scene:
     """Scene handle: BVH, triangles, materials, lights and textures on the GPU."""
 
     def __init__(self, sc: SceneArrays, lights: Optional[np.ndarray] = None,
-                 node_format: str = "q8"):
+                 node_format: str = "q8", bvh_width: int = 8):
         L = load()
         self.arrays = sc
         self._keep = []
@@ -84,8 +90,9 @@ class GB300Scene:
                          len(lights) if lights is not None else 0,
                          li.ctypes.data if lights is not None else None,
                          len(sc.textures), dims.ctypes.data if len(dims) else None,
-                         texels.ctypes.data, {"q8": _lib.NODES_Q8, "f32": _lib.NODES_F32}[node_format])
+                         texels.ctypes.data, NODE_FORMATS[node_format], bvh_width)
         self.node_format = node_format
+        self.bvh_width = bvh_width
         h = C.c_void_p()
         check(L.crt_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h
@@ -101,6 +108,11 @@ class GB300Scene:
         inf = SceneInfo()
         check(load().crt_scene_get_info(self.handle, C.byref(inf)))
         return inf
+
+    def set_bvh_width(self, width: int) -> None:
+        """Rebuild the BVH with 4 or 8 children per node (same geometry)."""
+        check(load().crt_scene_set_bvh_width(self.handle, width))
+        self.bvh_width = width
 
     def export_bvh(self):
         inf = self.info
@@ -134,27 +146,48 @@ class GB300Scene:
         return nodes, tris
 
 
+def make_options(max_depth: int = 6, seed: int = 1234, mode: str = "megakernel", view_id: int = 0,
+                 wave_paths: int = 0, flags: int = 0, wave_sets: int = 0, block_size: int = 0,
+                 stack_depth: int = 0, node_format: Optional[str] = None, queue_chunk: int = 0,
+                 options: Optional[RenderOptions] = None) -> RenderOptions:
+    """crt_render_options from keywords; `options` (e.g. the autotuner's
+    choice) overrides them all."""
+    if options is not None:
+        return options
+    opts = RenderOptions()
+    load().crt_render_options_default(C.byref(opts))
+    opts.max_depth = max_depth
+    opts.seed = seed
+    opts.view_id = view_id
+    opts.mode = {"megakernel": _lib.MODE_MEGAKERNEL, "wavefront": _lib.MODE_WAVEFRONT}[mode]
+    opts.wave_paths = wave_paths
+    opts.flags = flags
+    opts.wave_sets = wave_sets
+    opts.block_size = block_size
+    opts.stack_depth = stack_depth
+    opts.node_format = -1 if node_format is None else NODE_FORMATS[node_format]
+    opts.queue_chunk = queue_chunk
+    return opts
+
+
 class GB300Renderer:
     """Drop-in for ParallelRenderer (renderer.h:102-126) over the C ABI."""
 
     def __init__(self, scene: GB300Scene, width: int, height: int, samples: int,
                  camera: Optional[Camera] = None, max_depth: int = 6, seed: int = 1234,
                  mode: str = "megakernel", view_id: int = 0, wave_paths: int = 0,
-                 flags: int = 0):
+                 flags: int = 0, wave_sets: int = 0, block_size: int = 0,
+                 stack_depth: int = 0, node_format: Optional[str] = None,
+                 queue_chunk: int = 0, options: Optional[RenderOptions] = None):
         L = load()
         self.scene = scene
         self.width, self.height, self.samples = width, height, samples
         if camera is None:
             camera = camera_from_json(scene.arrays.camera, width, height)
         self.camera = camera
-        opts = RenderOptions()
-        L.crt_render_options_default(C.byref(opts))
-        opts.max_depth = max_depth
-        opts.seed = seed
-        opts.view_id = view_id
-        opts.mode = {"megakernel": _lib.MODE_MEGAKERNEL, "wavefront": _lib.MODE_WAVEFRONT}[mode]
-        opts.wave_paths = wave_paths
-        opts.flags = flags
+        opts = make_options(max_depth, seed, mode, view_id, wave_paths, flags, wave_sets,
+                            block_size, stack_depth, node_format, queue_chunk, options)
+        self.options = opts
         h = C.c_void_p()
         check(L.crt_render_create(scene.handle, C.byref(camera), width, height, C.byref(opts),
                                   C.byref(h)))
@@ -224,9 +257,114 @@ class GB300Renderer:
         for f in ("extension_rays", "extension_nodes", "extension_tris", "shadow_rays",
                   "shadow_nodes", "shadow_tris"):
             out[f] = getattr(p, f)
+        for f in ("extend_ms_by_bounce", "extend_rays_by_bounce", "shadow_ms_by_bounce",
+                  "shadow_rays_by_bounce"):
+            out[f] = list(getattr(p, f))
         return out
 
     def ray_counts(self):
         e, s = C.c_uint64(0), C.c_uint64(0)
         check(load().crt_render_ray_counts(self.handle, C.byref(e), C.byref(s)))
         return e.value, s.value
+
+    def adjoint(self, spp0: int, n_spp: int, adjoint_ptr: int, grad_kd_ptr: int, grad_ka_ptr: int,
+                stream: Optional[int] = None) -> None:
+        """Path-replay adjoint over device buffers (see crt_render_adjoint):
+        adds d<adjoint, radiance sum of samples [spp0, spp0+n_spp)>/d(kd, ka)
+        to the [num_materials][3] float buffers.  Runs on the handle's stream
+        (synchronize() before reading the gradients)."""
+        check(load().crt_render_adjoint(self.handle, spp0, n_spp, adjoint_ptr, grad_kd_ptr, grad_ka_ptr))
+
+
+class GB300Batch:
+    """Many camera views of one scene rendered together (crt_batch_*).
+    `views`: scenes.View items (camera spec, width, height, spp); view k uses
+    Philox view word view_ids[k] (default k)."""
+
+    def __init__(self, scene: GB300Scene, views, view_ids=None, **kw):
+        L = load()
+        self.scene = scene
+        self.views = list(views)
+        n = len(self.views)
+        arr = (View * n)()
+        for k, v in enumerate(self.views):
+            arr[k].camera = camera_from_json(v.camera, v.width, v.height)
+            arr[k].width, arr[k].height, arr[k].spp = v.width, v.height, v.spp
+            arr[k].view_id = k if view_ids is None else int(view_ids[k])
+        self._descs = arr
+        self.options = make_options(**kw)
+        h = C.c_void_p()
+        check(L.crt_batch_create(scene.handle, arr, n, C.byref(self.options), C.byref(h)))
+        self.handle = h
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            load().crt_render_destroy(self.handle)
+            self.handle = None
+
+    def __len__(self):
+        return len(self.views)
+
+    def render(self) -> None:
+        """Every view's own spp."""
+        check(load().crt_batch_render(self.handle))
+
+    def render_pass(self, n_spp: int) -> None:
+        check(load().crt_render_pass(self.handle, n_spp))
+
+    def synchronize(self) -> None:
+        check(load().crt_render_synchronize(self.handle))
+
+    def view_info(self, k: int):
+        d, s, off = View(), C.c_uint32(0), C.c_uint32(0)
+        check(load().crt_render_view_info(self.handle, k, C.byref(d), C.byref(s), C.byref(off)))
+        return dict(width=d.width, height=d.height, spp=d.spp, view_id=d.view_id,
+                    samples_rendered=s.value, pixel_offset=off.value)
+
+    def accum(self, k: int) -> np.ndarray:
+        v = self.views[k]
+        out = np.zeros((v.height * v.width, 3), np.float32)
+        check(load().crt_render_view_accum(self.handle, k, _ptr(out)))
+        return out
+
+    def resolve(self, k: int) -> np.ndarray:
+        v = self.views[k]
+        out = np.zeros((v.height, v.width, 4), np.uint8)
+        check(load().crt_render_view_resolve(self.handle, k, _ptr(out)))
+        return out
+
+    def set_stream(self, stream: int) -> None:
+        check(load().crt_render_set_stream(self.handle, stream))
+
+    def ray_counts(self):
+        e, s = C.c_uint64(0), C.c_uint64(0)
+        check(load().crt_render_ray_counts(self.handle, C.byref(e), C.byref(s)))
+        return e.value, s.value
+
+
+def autotune(scene: GB300Scene, width: int, height: int, camera: Optional[Camera] = None,
+             max_depth: int = 6, seed: int = 1234, trial_spp: int = 8, repeats: int = 3,
+             rounds: int = 2, tune_bvh_width: bool = True, start: Optional[RenderOptions] = None):
+    """Time short wavefront renders of this workload and return the fastest
+    launch options (a TuneResult; pass ``result.options`` to GB300Renderer).
+    With ``tune_bvh_width`` the scene's BVH may be rebuilt 4-wide."""
+    L = load()
+    if camera is None:
+        camera = camera_from_json(scene.arrays.camera, width, height)
+    if start is None:
+        start = RenderOptions()
+        L.crt_render_options_default(C.byref(start))
+        start.max_depth = max_depth
+        start.seed = seed
+    p = TuneParams()
+    L.crt_tune_params_default(C.byref(p))
+    p.trial_spp, p.repeats, p.rounds, p.tune_bvh_width = trial_spp, repeats, rounds, int(tune_bvh_width)
+    res = TuneResult()
+    check(L.crt_autotune(scene.handle, C.byref(camera), width, height, C.byref(start), C.byref(p),
+                         C.byref(res)))
+    scene.bvh_width = res.bvh_width
+    return res
+
+
+def options_dict(o: RenderOptions) -> dict:
+    return {name: getattr(o, name) for name, _ in o._fields_}

@@ -107,7 +107,9 @@ typedef struct {
     const uint32_t* texture_dims;  /* [num_textures][width, height] */
     const float* texels;           /* [sum(w*h)][rgb] linear floats, as
                                       stbi_loadf returns them */
-    uint32_t node_format;          /* crt_node_format */
+    uint32_t node_format;          /* crt_node_format renders use by default; both
+                                      encodings are uploaded */
+    uint32_t bvh_width;            /* children per node: 4 or 8 (0 = 8) */
 } crt_scene_desc;
 
 /* BVH node encoding on the device (same tree either way). */
@@ -135,6 +137,7 @@ typedef struct {
     uint64_t texture_bytes;
     float lights_area;
     float build_ms;
+    uint32_t bvh_width;        /* children per node of the current BVH: 4 or 8 */
 } crt_scene_info;
 
 /* ---- version / errors ------------------------------------------------ */
@@ -161,12 +164,20 @@ CRT_EXPORT int crt_scene_get_info(crt_scene scene, crt_scene_info* out);
  * triangle records [num_triangles][48 bytes] (v1.xyz + face index bits,
  * e1.xyz + 0, e2.xyz + 0).  Either pointer may be NULL. */
 CRT_EXPORT int crt_scene_export_bvh(crt_scene scene, void* nodes, void* triangles);
+/* Rebuilds the scene's BVH with 4 or 8 children per node from its own
+ * triangle records (the geometry is unchanged, so every query answers the
+ * same) and uploads it in place of the current one; the autotuner's BVH
+ * width axis.  Waits for the device to go idle before the old nodes are
+ * freed; render handles of the scene pick up the new BVH at their next pass.
+ * No reference counterpart: the reference's BVH is binary. */
+CRT_EXPORT int crt_scene_set_bvh_width(crt_scene scene, uint32_t bvh_width);
 /* The same BVH build on the host alone, without a device (inspection and
  * build statistics): call once with nodes/triangles NULL to learn
  * num_nodes, then again with buffers of num_nodes*80 and n*48 bytes.
+ * bvh_width: children per node, 4 or 8 (0 = 8).
  * Replaces constructBVH (src/geometry/bvh.cpp:65-77). */
-CRT_EXPORT int crt_bvh_build_host(const float* positions, uint32_t num_triangles, uint32_t* num_nodes,
-                       uint32_t* max_depth, void* nodes, void* triangles);
+CRT_EXPORT int crt_bvh_build_host(const float* positions, uint32_t num_triangles, uint32_t bvh_width,
+                                  uint32_t* num_nodes, uint32_t* max_depth, void* nodes, void* triangles);
 
 /* ---- ray queries ---------------------------------------------------------
  * Closest hit of a batch of rays; replaces intersectBVH
@@ -206,9 +217,19 @@ typedef struct {
     uint64_t seed;             /* Philox key */
     uint32_t view_id;          /* Philox counter word: separates views */
     uint32_t mode;             /* crt_mode */
-    uint32_t block_size;       /* 0 = library default */
-    uint32_t wave_paths;       /* wavefront: paths in flight, 0 = default */
+    uint32_t block_size;       /* wavefront traversal kernels: threads per block,
+                                  64, 128 or 256 (0 = 128) */
+    uint32_t wave_paths;       /* wavefront: paths in flight per wave set, 0 = default */
     uint32_t flags;            /* CRT_FLAG_* */
+    uint32_t wave_sets;        /* wavefront: waves in flight at once, each with its
+                                  own buffers and stream, 0..8 (0 = default 3) */
+    uint32_t stack_depth;      /* wavefront traversal kernels: stack entries per
+                                  thread kept in shared memory, 4..32 (0 = 16);
+                                  deeper entries go to local memory */
+    int32_t node_format;       /* crt_node_format, or -1 for the scene's format */
+    uint32_t queue_chunk;      /* wavefront traversal kernels: queue entries a warp
+                                  claims per fetch, 32, 64, 128 or 256 (0 = 32);
+                                  unused with CRT_FLAG_LANE_REFILL */
 } crt_render_options;
 
 CRT_EXPORT void crt_render_options_default(crt_render_options* opts);
@@ -241,6 +262,10 @@ typedef struct {
     uint64_t launches[6];
     uint64_t extension_rays, extension_nodes, extension_tris;
     uint64_t shadow_rays, shadow_nodes, shadow_tris;
+    double extend_ms_by_bounce[16];      /* bounces >= 15 add to the last entry */
+    uint64_t extend_rays_by_bounce[16];
+    double shadow_ms_by_bounce[16];
+    uint64_t shadow_rays_by_bounce[16];
 } crt_stage_profile;
 
 /* Renders n_spp more samples per pixel (like crt_render_pass, same result)
@@ -249,6 +274,61 @@ typedef struct {
  * extension and shadow traversal is re-run untimed in counting mode to
  * report node visits and triangle tests.  Wavefront handles only. */
 CRT_EXPORT int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out);
+
+/* ---- batched views ------------------------------------------------------
+ * No reference counterpart (the reference renders one camera per process).
+ * A batch is a render handle over many camera views of one scene, each with
+ * its own resolution, samples per pixel and Philox view word.  With
+ * CRT_MODE_WAVEFRONT, crt_batch_render runs every view's samples as one
+ * stream of waves: a wave packs whole sample layers or pixel ranges of
+ * several views, so small views share the GPU instead of each launching
+ * alone, and each wave replays the same captured CUDA graph.  With
+ * CRT_MODE_MEGAKERNEL the views render one after another (one launch
+ * sequence per view).  Either way view v's image equals, bit for bit, a
+ * single render of that view with view_id = views[v].view_id.
+ * crt_render_pass on a batch adds n_spp to every view; the single-view
+ * functions (crt_render_resolve, _accum, _samples_rendered, _set_camera) act
+ * on view 0, and crt_render_accum_device returns the accumulator of all
+ * views, view v at pixel offset crt_render_view_info(...).pixel_offset. */
+#define CRT_MAX_VIEWS 8192u
+typedef struct {
+    crt_camera camera;
+    uint32_t width, height;
+    uint32_t spp;              /* samples per pixel one crt_batch_render adds */
+    uint32_t view_id;          /* Philox counter word of this view */
+} crt_view;
+
+CRT_EXPORT int crt_batch_create(crt_scene scene, const crt_view* views, uint32_t num_views,
+                                const crt_render_options* opts, crt_render* out);
+/* Renders views[v].spp more samples per pixel of every view.  Asynchronous. */
+CRT_EXPORT int crt_batch_render(crt_render r);
+/* Size, spp and view word of a view (camera left zeroed), its samples so far
+ * and the offset of its first pixel in the accumulator; outputs may be NULL. */
+CRT_EXPORT int crt_render_view_info(crt_render r, uint32_t view, crt_view* desc, uint32_t* samples_rendered,
+                                    uint32_t* pixel_offset);
+CRT_EXPORT int crt_render_view_resolve(crt_render r, uint32_t view, uint8_t* host_rgba);
+CRT_EXPORT int crt_render_view_accum(crt_render r, uint32_t view, float* host_rgb);
+
+/* ---- adjoint (differentiable rendering) -----------------------------------
+ * No reference counterpart (the reference computes no derivatives).
+ * Gradient of  Phi = sum over pixels p, channels c of adjoint[p][c] * S[p][c],
+ * S being the radiance sum that samples [spp0, spp0 + n_spp) add to each
+ * pixel (the samples crt_render_pass renders there), with respect to every
+ * material's kd (diffuse albedo; diffuse vertices of untextured materials)
+ * and ka (emission as given in crt_material).  For an image loss L(I) with
+ * I = accum / spp, pass adjoint = dL/dI / spp.
+ * Path-replay backpropagation: each path is traced twice from the same
+ * Philox counters, first for its radiance, then again turning every vertex
+ * into gradient terms, so nothing per vertex is stored; Russian roulette's
+ * survival probability counts as a constant.  Gradients are summed per warp
+ * and block before global atomics.  Always the wavefront form.
+ * d_adjoint: device float4 per pixel of every view (the layout of
+ * crt_render_accum_device; .w ignored).  d_grad_kd, d_grad_ka: device float
+ * [num_materials][3], ADDED to.  At most 1024 materials.  Asynchronous on the
+ * handle's stream; the accumulator and sample counts do not change. */
+CRT_EXPORT int crt_render_adjoint(crt_render r, uint32_t spp0, uint32_t n_spp, const float* d_adjoint,
+                                  float* d_grad_kd, float* d_grad_ka);
+
 /* ---- allocation-free tile render ----------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
  * allocate device memory while rendering, such as a host application that
@@ -281,6 +361,39 @@ CRT_EXPORT int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
 
 /* Extension and shadow rays traced by the passes since the last reset. */
 CRT_EXPORT int crt_render_ray_counts(crt_render r, uint64_t* extension_rays, uint64_t* shadow_rays);
+
+/* ---- autotuner ------------------------------------------------------
+ * No reference counterpart: the reference's launch shape is fixed at
+ * compile time (16x16 blocks, renderer.cu:543-551).  crt_autotune times
+ * short wavefront renders of the given scene, camera and image size and
+ * searches, by coordinate descent, the options that change speed but not
+ * the image: node_format, block_size, stack_depth, queue_chunk, wave_sets,
+ * wave_paths, CRT_FLAG_LANE_REFILL and (tune_bvh_width) the BVH width.
+ * The device must be otherwise idle for the timings to mean anything.  With
+ * tune_bvh_width the scene's BVH is rebuilt (crt_scene_set_bvh_width) and
+ * the faster width is left in place. */
+typedef struct {
+    uint32_t trial_spp;        /* samples per pixel of each timed render (0 = 8) */
+    uint32_t repeats;          /* timed renders per candidate, fastest kept (0 = 3) */
+    uint32_t rounds;           /* coordinate-descent sweeps at most (0 = 2) */
+    uint32_t tune_bvh_width;   /* nonzero: also try the other BVH width */
+    uint64_t max_wave_bytes;   /* skip candidates whose path state exceeds this
+                                  (0 = 8 GiB) */
+} crt_tune_params;
+
+typedef struct {
+    crt_render_options options;  /* fastest options (mode = wavefront, defaults spelled out) */
+    uint32_t bvh_width;          /* BVH width left in the scene */
+    uint32_t candidates;         /* distinct candidates timed */
+    float ms_per_spp;            /* fastest: milliseconds per sample per pixel */
+    float start_ms_per_spp;      /* the starting options, for comparison */
+    float tune_ms;               /* wall time spent tuning */
+} crt_tune_result;
+
+CRT_EXPORT void crt_tune_params_default(crt_tune_params* params);
+CRT_EXPORT int crt_autotune(crt_scene scene, const crt_camera* camera, uint32_t width, uint32_t height,
+                            const crt_render_options* start, const crt_tune_params* params,
+                            crt_tune_result* out);
 
 #ifdef __cplusplus
 }

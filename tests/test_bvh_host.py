@@ -19,8 +19,8 @@ def _decode(node, slot):
     return lo, hi
 
 
-def _check(positions):
-    nodes, tris, depth = bvh_build_host(positions)
+def _check(positions, width=8):
+    nodes, tris, depth = bvh_build_host(positions, width)
     n = len(positions)
     assert depth <= MAX_LEVELS
     assert sorted(tris["face"].tolist()) == list(range(n))
@@ -29,6 +29,8 @@ def _check(positions):
     f = tris["face"]
     assert np.array_equal(tris["v1"], positions[f, 0])
     assert np.array_equal(tris["e1"], positions[f, 1] - positions[f, 0])
+    used = np.count_nonzero(nodes["meta"], axis=1)
+    assert np.all(used >= 1) and np.all(used <= width)
     parent_boxes = {0: (np.full(3, -np.inf), np.full(3, np.inf))}
     seen_internal = 0
     for i, node in enumerate(nodes):
@@ -91,3 +93,15 @@ def test_empty_scene_is_an_error():
     from cudart_gb300 import CrtError
     with pytest.raises(CrtError):
         bvh_build_host(np.zeros((0, 3, 3), np.float32))
+
+
+def test_four_wide_bvh():
+    n8, d8 = _check(scenes.mixed_mid(subdiv=3).positions, width=8)
+    n4, d4 = _check(scenes.mixed_mid(subdiv=3).positions, width=4)
+    assert len(n4) > len(n8) and d4 >= d8
+
+
+def test_bad_width_is_an_error():
+    from cudart_gb300 import CrtError
+    with pytest.raises(CrtError):
+        bvh_build_host(scenes.cornell_box().positions, width=6)

@@ -64,6 +64,33 @@ def test_f32_nodes_render_identically(cuda, mode):
     assert np.array_equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("shape", [dict(block_size=64), dict(block_size=256),
+                                   dict(stack_depth=4), dict(stack_depth=32, block_size=256),
+                                   dict(node_format="f32"), dict(wave_sets=1), dict(wave_sets=8)])
+def test_launch_shape_does_not_change_results(cuda, shape):
+    """Block size, shared stack depth, per-render node format and the
+    number of wave sets are scheduling choices: the image is unchanged."""
+    sc = scenes.large_textured(width=96, height=54, grid=64, tex_size=64, n_spheres=12,
+                               sphere_subdiv=2)
+    g = GB300Scene(sc)
+    out = []
+    for kw in ({}, shape):
+        r = GB300Renderer(g, sc.width, sc.height, 8, max_depth=8, mode="wavefront",
+                          wave_paths=1 << 14, **kw)
+        r.render()
+        out.append(r.accum())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_four_wide_bvh_renders_identically(cuda):
+    sc = scenes.mixed_mid(width=128, height=72, subdiv=3)
+    a = GB300Renderer(GB300Scene(sc), 128, 72, 8, max_depth=8, mode="wavefront")
+    b = GB300Renderer(GB300Scene(sc, bvh_width=4), 128, 72, 8, max_depth=8, mode="wavefront")
+    a.render()
+    b.render()
+    assert np.array_equal(a.accum(), b.accum())
+
+
 def test_progressive_passes_equal_single(cuda):
     sc = scenes.cornell_box(width=64, height=64)
     g = GB300Scene(sc)

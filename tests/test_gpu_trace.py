@@ -11,8 +11,8 @@ from cudart_gb300 import GB300Scene, scenes
 pytestmark = pytest.mark.gpu
 
 
-def _check(cuda, sc, rays, brute=True, node_format="q8"):
-    g = GB300Scene(sc, node_format=node_format)
+def _check(cuda, sc, rays, brute=True, node_format="q8", bvh_width=8):
+    g = GB300Scene(sc, node_format=node_format, bvh_width=bvh_width)
     idx, t, uv = g.trace_closest(cuda.from_numpy(rays).cuda())
     o = oracle.OracleScene(sc)
     oi, ot, ouv = o.closest_hit(rays, brute=brute)
@@ -52,6 +52,12 @@ def test_cornell_ties_lowest_index(cuda):
 def test_mixed_scene_bvh_oracle(cuda, fmt):
     sc = scenes.mixed_mid(subdiv=3)
     _check(cuda, sc, random_rays(20000, 2), node_format=fmt)
+
+
+@pytest.mark.parametrize("fmt", ["q8", "f32"])
+def test_four_wide_bvh(cuda, fmt):
+    sc = scenes.mixed_mid(subdiv=3)
+    _check(cuda, sc, random_rays(20000, 5), node_format=fmt, bvh_width=4)
 
 
 @pytest.mark.parametrize("fmt", ["q8", "f32"])
