@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Msamples/s at 1080p, equal RMSE, vs plain kernel; adjoint/forward time ratio"
 WORKLOAD = ("large_textured 1920x1080 256spp depth8: 1024^2-vertex heightfield + 1024^2 RGBA8 "
             "texture, 64 glass/mirror icospheres (subdiv 3), 4 quad lights, 2,174,986 triangles")
-NODE_BYTES, TRI_BYTES = 80, 48
+NODE_BYTES, F32_NODE_BYTES, TRI_BYTES = 80, 208, 48
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -158,10 +158,136 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def batched_views_leg(args, torch, stream):
+    """C4: the 64 views of the batched-views generator over the mixed scene
+    in one wavefront batch (autotuned launch options incl. BVH width) against
+    the same views as 64 sequential plain-kernel renders.  spp / spp_div per
+    view keeps the leg to a few seconds; both arms render the same samples."""
+    import dataclasses
+    from cudart_gb300 import GB300Batch, GB300Scene, autotune, options_dict, scenes
+    sc = scenes.mixed_mid()
+    views = [dataclasses.replace(v, spp=max(1, v.spp // args.c4_spp_div))
+             for v in scenes.batched_views(base=sc).views]
+    samples = sum(v.width * v.height * v.spp for v in views)
+    g = GB300Scene(sc)
+    t0 = time.perf_counter()
+    tune = autotune(g, 1024, 1024, max_depth=sc.max_depth, trial_spp=4, repeats=2, rounds=1,
+                    tune_bvh_width=True)
+    tune_s = time.perf_counter() - t0
+    opts = tune.options
+    out = {"workload": f"mixed_mid (102,412 triangles), 64 views r=12, resolutions "
+                       f"{{256^2, 512^2, 768x432, 1024^2}}, spp {{16, 64, 256}} / {args.c4_spp_div}, depth 8",
+           "samples_per_step": samples,
+           "autotuned": {k: v for k, v in options_dict(opts).items() if k not in ("seed", "max_depth", "view_id")},
+           "bvh_width": tune.bvh_width, "tune_seconds": round(tune_s, 2),
+           "tune_candidates": tune.candidates}
+    res = {}
+    for name, kw in (("batched_wavefront", dict(options=opts)), ("sequential_plain", dict(mode="megakernel"))):
+        b = GB300Batch(g, views, max_depth=sc.max_depth, **kw)
+        b.set_stream(stream.cuda_stream)
+        b.render_pass(1)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        b.render()
+        e.record(stream)
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e)
+        res[name] = {"ms": round(ms, 2), "msamples_per_s": round(samples / (ms * 1e-3) / 1e6, 2)}
+        del b
+    out.update(res)
+    out["speedup"] = round(res["batched_wavefront"]["msamples_per_s"] / res["sequential_plain"]["msamples_per_s"], 3)
+    return out
+
+
+def adjoint_leg(args, torch, stream):
+    """C5: Cornell shell + 32 boxes at 512^2, 64 spp per iteration, depth 6.
+    adjoint/forward: one adjoint pass (primal trace + replay, both on the GPU)
+    against one forward wavefront pass of the same 64 spp (CUDA events, median
+    of 5).  Then the material inversion: target 1024 spp with the true
+    albedos, start at albedo 0.5 for the 32 boxes, L2 image loss, Adam at
+    lr 1e-2 for `inversion_iters` iterations, gradients from the adjoint on
+    samples independent of the iteration's image (the same samples would
+    correlate the residual with its derivative and bias the gradient)."""
+    import numpy as np
+    from cudart_gb300 import GB300Renderer, GB300Scene, scenes
+    sc = scenes.material_inversion()
+    g = GB300Scene(sc)
+    n_mats = len(sc.materials)
+    kd_true = np.array([m.kd for m in sc.materials], np.float32)
+    boxes = np.arange(4, n_mats)
+    npix = sc.width * sc.height
+    r = GB300Renderer(g, sc.width, sc.height, sc.spp, max_depth=sc.max_depth, seed=77, mode="wavefront")
+    r.set_stream(stream.cuda_stream)
+    # target image: 1024 spp with the true albedos (its own sample range)
+    r.restart(1 << 24)
+    r.render(1024)
+    target = torch.from_numpy(r.accum()).cuda() / 1024
+    adj = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    gkd = torch.zeros((n_mats, 3), dtype=torch.float32, device="cuda")
+    gka = torch.zeros((n_mats, 3), dtype=torch.float32, device="cuda")
+    adj[:, :3] = 1.0
+    fw, bw = [], []
+    for k in range(6):
+        r.restart(k * sc.spp)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        r.render(sc.spp)
+        e.record(stream)
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s2.record(stream)
+        r.adjoint(k * sc.spp, sc.spp, adj.data_ptr(), gkd.data_ptr(), gka.data_ptr())
+        e2.record(stream)
+        torch.cuda.synchronize()
+        if k:
+            fw.append(s.elapsed_time(e))
+            bw.append(s2.elapsed_time(e2))
+    f_ms, a_ms = statistics.median(fw), statistics.median(bw)
+    out = {"workload": "material_inversion: Cornell shell + 32 diffuse boxes (396 triangles), "
+                       "512x512, 64 spp, depth 6",
+           "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3), "ratio": round(a_ms / f_ms, 3),
+           "roulette": "survival probability held constant (unbiased gradient of the expected image)"}
+    # inversion
+    kd = kd_true.copy()
+    kd[boxes] = 0.5
+    m1 = np.zeros_like(kd)
+    m2 = np.zeros_like(kd)
+    b1, b2, lr, eps = 0.9, 0.999, 1e-2, 1e-8
+    err0 = float(np.sqrt(np.mean((kd[boxes] - kd_true[boxes]) ** 2)))
+    t0 = time.perf_counter()
+    for it in range(args.inversion_iters):
+        g.set_materials(kd=kd)
+        r.restart(it * sc.spp)
+        r.render(sc.spp)
+        img = torch.from_numpy(r.accum()).cuda() / sc.spp
+        diff = img - target
+        loss = float((diff ** 2).sum())
+        adj[:, :3] = 2.0 * diff / sc.spp
+        gkd.zero_()
+        gka.zero_()
+        r.adjoint((1 << 23) + it * sc.spp, sc.spp, adj.data_ptr(), gkd.data_ptr(), gka.data_ptr())
+        r.synchronize()
+        grad = gkd.cpu().numpy()
+        grad[np.setdiff1d(np.arange(n_mats), boxes)] = 0.0
+        m1 = b1 * m1 + (1 - b1) * grad
+        m2 = b2 * m2 + (1 - b2) * grad * grad
+        step = lr * (m1 / (1 - b1 ** (it + 1))) / (np.sqrt(m2 / (1 - b2 ** (it + 1))) + eps)
+        kd = np.clip(kd - step, 0.01, 0.99).astype(np.float32)
+        if it == 0:
+            loss0 = loss
+    g.set_materials(kd=kd_true)
+    out["inversion"] = {"iterations": args.inversion_iters, "lr": lr, "loss_first": round(loss0, 4),
+                        "loss_last": round(loss, 4),
+                        "albedo_rmse_start": round(err0, 4),
+                        "albedo_rmse_end": round(float(np.sqrt(np.mean((kd[boxes] - kd_true[boxes]) ** 2))), 4),
+                        "seconds": round(time.perf_counter() - t0, 2)}
+    return out
+
+
 def run_gb300(args):
     import numpy as np
     import torch
-    from cudart_gb300 import GB300Renderer, GB300Scene, scenes
+    from cudart_gb300 import GB300Renderer, GB300Scene, autotune, options_dict, scenes
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -186,9 +312,25 @@ def run_gb300(args):
     torch.cuda.set_stream(stream)
     scene = GB300Scene(sc)
     info = scene.info
-    # each rank renders its own Philox streams of the same frame (view_id = rank)
-    wf = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
-                       mode="wavefront", view_id=rank)
+    # launch options: the autotuner on this frame (untimed; BVH width kept at
+    # 8, the 4-wide tree of this scene measured slower)
+    tuned = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tune = autotune(scene, sc.width, sc.height, max_depth=sc.max_depth, trial_spp=8, repeats=2,
+                        rounds=1, tune_bvh_width=False)
+        tuned = {"options": {k: v for k, v in options_dict(tune.options).items()
+                             if k not in ("seed", "max_depth", "view_id")},
+                 "candidates": tune.candidates, "seconds": round(time.perf_counter() - t0, 2),
+                 "start_ms_per_spp": round(tune.start_ms_per_spp, 3),
+                 "tuned_ms_per_spp": round(tune.ms_per_spp, 3)}
+        opts = tune.options
+        opts.seed, opts.view_id = 1234, rank
+        wf = GB300Renderer(scene, sc.width, sc.height, spp, options=opts)
+    else:
+        # each rank renders its own Philox streams of the same frame (view_id = rank)
+        wf = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
+                           mode="wavefront", view_id=rank)
     wf.set_stream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -235,22 +377,23 @@ def run_gb300(args):
     mk_ms = sum(timed_steps(mk, k_plain)) / k_plain
     identical = bool(np.array_equal(mk.accum(), wf_acc))
     plain_value = npix * spp / (mk_ms * 1e-3) / 1e6
+    del mk
 
     out = None
     if rank == 0:
         # roofline: profiled pass of 8 spp (per-launch events, counted fetches)
-        prof_r = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
-                               mode="wavefront")
+        prof_r = GB300Renderer(scene, sc.width, sc.height, spp, options=wf.options)
         prof_r.set_stream(stream.cuda_stream)
         prof = prof_r.profile_pass(8)
         stages = ("generate", "extend", "shade", "shadow", "accumulate", "bookkeeping")
         dom = max(stages, key=lambda s: prof[f"{s}_ms"])
         peak, peak_kind = measured_peaks()
+        node_bytes = NODE_BYTES if wf.options.node_format != 1 else F32_NODE_BYTES
         roof = {}
         for stage, rays, nodes, tris in (("extend", "extension_rays", "extension_nodes", "extension_tris"),
                                          ("shadow", "shadow_rays", "shadow_nodes", "shadow_tris")):
             launches = prof[f"{stage}_launches"]
-            alg = prof[nodes] * NODE_BYTES + prof[tris] * TRI_BYTES
+            alg = prof[nodes] * node_bytes + prof[tris] * TRI_BYTES
             ms_l = prof[f"{stage}_ms"] / launches
             gbs = alg / launches / (ms_l * 1e-3) / 1e9
             roof[stage] = {"kernel": "wf_" + stage, "bytes_per_launch": alg / launches,
@@ -267,31 +410,41 @@ def run_gb300(args):
         roofline = {"bound": "hbm", "kernel": main["kernel"], "achieved": round(main["gbs"], 1),
                     "peak": peak, "unit": "GB/s", "frac": round(main["gbs"] / peak, 4),
                     "traffic": traffic, "peak_kind": f"{peak_kind} (HBM copy)",
-                    "algorithmic_bytes": "nodes visited x 80 B + triangles tested x 48 B per ray",
+                    "algorithmic_bytes": f"nodes visited x {node_bytes} B + triangles tested x 48 B per ray",
                     "stage_ms": {s: round(prof[f"{s}_ms"], 2) for s in stages},
+                    "profile_spp": 8,
+                    "extend_rays_by_bounce": prof["extend_rays_by_bounce"][:sc.max_depth],
+                    "extend_ms_by_bounce": [round(x, 3) for x in prof["extend_ms_by_bounce"][:sc.max_depth]],
                     "stages": {k: {kk: (round(vv, 3) if isinstance(vv, float) else vv)
                                    for kk, vv in v.items()} for k, v in roof.items()}}
         del prof_r
 
         # e2e: host arrays -> host image through the public API
         h2d = int(info.node_bytes + info.triangle_bytes + info.shading_bytes + info.texture_bytes)
-        e2e_t = []
+        e2e_t, create_t, build_t = [], [], []
         for k in range(1 + max(1, min(args.steps, 2))):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             s2 = GB300Scene(sc)
-            r2 = GB300Renderer(s2, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
-                               mode="wavefront")
+            t1 = time.perf_counter()
+            r2 = GB300Renderer(s2, sc.width, sc.height, spp, options=wf.options)
             r2.render(spp)
             img = r2.copy_image_bytes()
             e2e_t.append(time.perf_counter() - t0)
+            create_t.append(t1 - t0)
+            build_t.append(s2.info.build_ms * 1e-3)
             del r2, s2
         e2e_s = statistics.mean(e2e_t[1:])
         e2e = {"value": round(npix * spp / e2e_s / 1e6, 3), "unit": "Msamples/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(img.nbytes),
                "seconds_per_step": round(e2e_s, 4),
+               "scene_create_s": round(statistics.mean(create_t[1:]), 4),
+               "scene_build_s": round(statistics.mean(build_t[1:]), 4),
                "region": "crt_scene_create (host BVH build + uploads) + crt_render_create + "
                          "crt_render_pass(256) + crt_render_resolve to host RGBA8"}
+
+        c4 = batched_views_leg(args, torch, stream) if world == 1 and not args.no_extra else None
+        c5 = adjoint_leg(args, torch, stream) if world == 1 and not args.no_extra else None
 
         cpu = None
         if world == 1 and not args.no_cpu:
@@ -305,24 +458,26 @@ def run_gb300(args):
                    "kind": "port",
                    "sample": (f"{len(px)} stratified pixels x 1 spp" if px is not None
                               else f"full frame x {k_spp} spp") + f" of the 1920x1080 frame, {dt:.1f} s"}
-        waves = math.ceil(spp / max(1, (1 << 22) // npix)) if npix <= (1 << 22) else spp * math.ceil(npix / (1 << 22))
+        cap = wf.options.wave_paths or (1 << 22)
+        waves = math.ceil(spp / max(1, cap // npix)) if npix <= cap else spp * math.ceil(npix / cap)
         launches = args.steps * waves * (3 + 4 * sc.max_depth)
         out = {
             "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator: heightfield value noise, procedural texture)",
-            "config": {"workload": WORKLOAD, "mode": "wavefront (CUDA-graph waves of 4M paths)",
+            "config": {"workload": WORKLOAD, "mode": "wavefront (CUDA-graph waves, concurrent wave sets)",
                        "width": sc.width, "height": sc.height, "spp": spp, "max_depth": sc.max_depth,
                        "triangles": info.num_triangles, "bvh_nodes": info.num_nodes,
-                       "bvh_depth": info.max_depth,
+                       "bvh_depth": info.max_depth, "autotune": tuned,
                        "l2": "flushed before every step (256 MiB write); scene buffers > L2"},
             "plain_kernel": {"value": round(plain_value, 3), "ms_per_step": round(mk_ms, 3),
-                             "accum_identical_to_wavefront": identical},
+                             "node_format": "q8", "accum_identical_to_wavefront": identical},
             "speedup_vs_plain": round(value / world / plain_value, 3),
             "mrays_per_s": round(value * rays_per_sample, 1),
             "rays_per_sample": round(rays_per_sample, 3),
-            "adjoint_forward_ratio": None,
+            "adjoint_forward_ratio": c5["ratio"] if c5 else None,
+            "batched_views": c4, "adjoint": c5,
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
             "cpu_baseline": cpu,
         }
@@ -342,6 +497,10 @@ def main():
     ap.add_argument("--spp", type=int, default=256)
     ap.add_argument("--small", action="store_true", help="480x270 reduced scene (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true", help="default launch options, no autotuner")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched-views and adjoint legs")
+    ap.add_argument("--c4-spp-div", type=int, default=4, help="batched views: spp divisor")
+    ap.add_argument("--inversion-iters", type=int, default=200)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -53,7 +53,8 @@ class SceneDesc(C.Structure):
                 ("num_materials", C.c_uint32), ("materials", C.c_void_p),
                 ("num_lights", C.c_uint32), ("light_indices", C.c_void_p),
                 ("num_textures", C.c_uint32), ("texture_dims", C.c_void_p),
-                ("texels", C.c_void_p), ("node_format", C.c_uint32), ("bvh_width", C.c_uint32)]
+                ("texels", C.c_void_p), ("node_format", C.c_uint32), ("bvh_width", C.c_uint32),
+                ("flags", C.c_uint32)]
 
 
 NODES_Q8 = 0
@@ -83,7 +84,8 @@ class RenderOptions(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("seed", C.c_uint64), ("view_id", C.c_uint32),
                 ("mode", C.c_uint32), ("block_size", C.c_uint32), ("wave_paths", C.c_uint32),
                 ("flags", C.c_uint32), ("wave_sets", C.c_uint32), ("stack_depth", C.c_uint32),
-                ("node_format", C.c_int32), ("queue_chunk", C.c_uint32)]
+                ("node_format", C.c_int32), ("queue_chunk", C.c_uint32), ("top_nodes", C.c_uint32),
+                ("refill_busy", C.c_uint32)]
 
 
 class TuneParams(C.Structure):
@@ -96,6 +98,9 @@ class TuneResult(C.Structure):
                 ("ms_per_spp", C.c_float), ("start_ms_per_spp", C.c_float), ("tune_ms", C.c_float)]
 
 
+ADJOINT_EXACT_ROULETTE = 1
+SCENE_EDGES = 1
+SCENE_KA_SCALED = 2
 FLAG_LANE_REFILL = 1
 FLAG_SPLIT_LEAF = 2
 
@@ -112,6 +117,7 @@ SIGNATURES = {
     "crt_scene_export_bvh": (C.c_int, [P, P, P]),
     "crt_bvh_build_host": (C.c_int, [P, U32, U32, P, P, P, P]),
     "crt_scene_set_bvh_width": (C.c_int, [P, U32]),
+    "crt_scene_set_materials": (C.c_int, [P, P, U32]),
     "crt_trace_closest": (C.c_int, [P, P, U32, P, P, P, P]),
     "crt_trace_counts": (C.c_int, [P, P, U32, P, P, P]),
     "crt_render_options_default": (None, [P]),
@@ -132,7 +138,11 @@ SIGNATURES = {
     "crt_render_profile_pass": (C.c_int, [P, U32, P]),
     "crt_render_tile_noalloc": (C.c_int, [P, P, U32, U32, P, U32, U32, U32, U32, P, P]),
     "crt_batch_create": (C.c_int, [P, P, U32, P, P]),
-    "crt_render_adjoint": (C.c_int, [P, U32, U32, P, P, P]),
+    "crt_render_adjoint": (C.c_int, [P, U32, U32, P, P, P, U32]),
+    "crt_render_restart": (C.c_int, [P, U32]),
+    "crt_render_resolve_device": (C.c_int, [P, P]),
+    "crt_render_resolve_async": (C.c_int, [P, P]),
+    "crt_render_load_accum": (C.c_int, [P, U32, P, U32, U32]),
     "crt_batch_render": (C.c_int, [P]),
     "crt_render_view_info": (C.c_int, [P, U32, P, P, P]),
     "crt_render_view_resolve": (C.c_int, [P, U32, P]),

@@ -43,51 +43,104 @@ struct Builder {
     const Box* tbox;
     const float* cent;     // [n][3]
     uint32_t* idx;
+    unsigned hw_threads;
 
-    // Binned SAH split of idx[start, end); returns mid (start < mid < end).
-    uint32_t split(uint32_t start, uint32_t end, const Box& cb) const {
-        float best_cost = FLT_MAX;
-        int best_axis = -1, best_bin = 0;
+    // Bins of idx[s, e) along every axis with a positive centroid extent.
+    struct Bins {
+        Box bb[3][kBins];
+        uint32_t cnt[3][kBins];
+        void reset() {
+            for (int ax = 0; ax < 3; ++ax)
+                for (int b = 0; b < kBins; ++b) {
+                    bb[ax][b].reset();
+                    cnt[ax][b] = 0;
+                }
+        }
+        void merge(const Bins& o) {
+            for (int ax = 0; ax < 3; ++ax)
+                for (int b = 0; b < kBins; ++b) {
+                    bb[ax][b].grow(o.bb[ax][b]);
+                    cnt[ax][b] += o.cnt[ax][b];
+                }
+        }
+    };
+
+    // One axis at a time: each pass streams idx[s, e) once.
+    void bin_range(uint32_t s, uint32_t e, const Box& cb, const float scale[3], Bins& B) const {
         for (int ax = 0; ax < 3; ++ax) {
-            float ext = cb.hi[ax] - cb.lo[ax];
-            if (!(ext > 0.f)) continue;
-            float scale = kBins / ext;
-            Box bb[kBins];
-            uint32_t cnt[kBins] = {0};
-            for (int b = 0; b < kBins; ++b) bb[b].reset();
-            for (uint32_t i = start; i < end; ++i) {
-                uint32_t t = idx[i];
-                int b = std::min(kBins - 1, (int)((cent[3 * t + ax] - cb.lo[ax]) * scale));
+            if (!(scale[ax] > 0.f)) continue;
+            const float lo = cb.lo[ax], sc = scale[ax];
+            Box* bb = B.bb[ax];
+            uint32_t* cnt = B.cnt[ax];
+            for (uint32_t i = s; i < e; ++i) {
+                const uint32_t t = idx[i];
+                int b = std::min(kBins - 1, (int)((cent[3 * t + ax] - lo) * sc));
                 b = std::max(b, 0);
                 cnt[b]++;
                 bb[b].grow(tbox[t]);
             }
+        }
+    }
+
+    // Binned SAH split of idx[start, end); returns mid (start < mid < end).
+    // Large ranges are binned by several threads; boxes merge by min / max
+    // and counts by sums, so the split does not depend on the thread count.
+    uint32_t split(uint32_t start, uint32_t end, const Box& cb) const {
+        float scale[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            const float ext = cb.hi[ax] - cb.lo[ax];
+            scale[ax] = ext > 0.f ? kBins / ext : 0.f;
+        }
+        Bins B;
+        B.reset();
+        const uint32_t n = end - start;
+        const unsigned parts = n >= (1u << 16) ? std::min<unsigned>(hw_threads, n >> 15) : 1u;
+        if (parts > 1) {
+            std::vector<Bins> part(parts);
+            std::vector<std::thread> pool;
+            for (unsigned p = 0; p < parts; ++p) {
+                const uint32_t s = start + (uint32_t)((uint64_t)n * p / parts);
+                const uint32_t e = start + (uint32_t)((uint64_t)n * (p + 1) / parts);
+                pool.emplace_back([&, p, s, e] {
+                    part[p].reset();
+                    bin_range(s, e, cb, scale, part[p]);
+                });
+            }
+            for (std::thread& t : pool) t.join();
+            for (const Bins& q : part) B.merge(q);
+        } else {
+            bin_range(start, end, cb, scale, B);
+        }
+        float best_cost = FLT_MAX;
+        int best_axis = -1, best_bin = 0;
+        for (int ax = 0; ax < 3; ++ax) {
+            if (!(scale[ax] > 0.f)) continue;
             float left_area[kBins];
             uint32_t left_cnt[kBins];
             Box acc;
             acc.reset();
             uint32_t c = 0;
             for (int b = 0; b < kBins; ++b) {
-                acc.grow(bb[b]);
-                c += cnt[b];
+                acc.grow(B.bb[ax][b]);
+                c += B.cnt[ax][b];
                 left_area[b] = acc.half_area();
                 left_cnt[b] = c;
             }
             acc.reset();
             c = 0;
             for (int b = kBins - 1; b > 0; --b) {
-                acc.grow(bb[b]);
-                c += cnt[b];
+                acc.grow(B.bb[ax][b]);
+                c += B.cnt[ax][b];
                 if (left_cnt[b - 1] == 0 || c == 0) continue;
                 float cost = left_area[b - 1] * left_cnt[b - 1] + acc.half_area() * c;
                 if (cost < best_cost) { best_cost = cost; best_axis = ax; best_bin = b - 1; }
             }
         }
         if (best_axis < 0) return start + (end - start) / 2;   // coincident centroids
-        float scale = kBins / (cb.hi[best_axis] - cb.lo[best_axis]);
-        float lo = cb.lo[best_axis];
+        const float sc = scale[best_axis];
+        const float lo = cb.lo[best_axis];
         uint32_t* mid = std::partition(idx + start, idx + end, [&](uint32_t t) {
-            int b = std::min(kBins - 1, (int)((cent[3 * t + best_axis] - lo) * scale));
+            int b = std::min(kBins - 1, (int)((cent[3 * t + best_axis] - lo) * sc));
             return std::max(b, 0) <= best_bin;
         });
         uint32_t m = (uint32_t)(mid - idx);
@@ -145,6 +198,24 @@ struct Builder {
     }
 };
 
+// Runs f(begin, end) over [0, n) split across the hardware threads.
+template <class F>
+void parallel_for(size_t n, F f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    if (n < 8192 || hw == 1) {
+        f(size_t(0), n);
+        return;
+    }
+    const size_t chunk = (n + hw - 1) / hw;
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < hw; ++t) {
+        const size_t b = t * chunk, e = std::min(n, b + chunk);
+        if (b >= e) break;
+        pool.emplace_back(f, b, e);
+    }
+    for (std::thread& t : pool) t.join();
+}
+
 // Smallest e with ext <= 255 * 2^e, clamped to the normal float range.
 int scale_exponent(double ext) {
     if (!(ext > 0.0)) return -126;
@@ -185,7 +256,7 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
     }
     std::vector<uint32_t> idx(n);
     for (uint32_t i = 0; i < n; ++i) idx[i] = i;
-    Builder b{tbox.data(), cent.data(), idx.data()};
+    Builder b{tbox.data(), cent.data(), idx.data(), std::max(1u, std::thread::hardware_concurrency())};
     std::vector<Node2> n2;
     n2.reserve(2ull * n);
     unsigned hw = std::max(1u, std::thread::hardware_concurrency());
@@ -193,29 +264,33 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
     while ((1u << par_depth) < hw * 2 && par_depth < 8) ++par_depth;
     int32_t root = b.build(0, n, n2, par_depth);
 
-    // ---- collapse to 8-wide, breadth first --------------------------------
-    struct Item { int32_t n2; uint32_t depth; };
-    std::vector<Item> queue;
-    queue.push_back({root, 1});
-    out.nodes.clear();
-    out.tris.clear();
-    out.tris.reserve(n);
-    out.max_depth = 0;
-    out.margin = margin;
-    out.fnodes.clear();
-    out.fnodes_ok = true;
-    out.nodes.resize(1);
-    for (size_t qi = 0; qi < queue.size(); ++qi) {
-        const Item it = queue[qi];
-        out.max_depth = std::max(out.max_depth, it.depth);
-        if (it.depth > max_levels) { *msg = "BVH deeper than the traversal stack allows"; return false; }
-        int32_t ch[8];
+    // ---- collapse to max_children-wide nodes, breadth-first layout --------
+    // 1. (serial, cheap) each wide node takes its BVH2 node's children and
+    //    keeps opening the internal child of largest area;
+    // 2. (parallel) children are assigned to slots by octant;
+    // 3. (serial, cheap) breadth-first numbering in slot order gives each
+    //    node its child and triangle base;
+    // 4. (parallel) nodes are encoded and triangle records written.
+    struct Wide {
+        int32_t nch;
+        int32_t ch[8];       // BVH2 children
+        int32_t rec[8];      // wide record of an internal child, else -1
+        int32_t slot_of[8];
+        uint32_t depth;
+    };
+    std::vector<Wide> recs;
+    recs.reserve(n / 2 + 1);
+    auto add_record = [&](int32_t node2, uint32_t depth) {
+        Wide w;
+        std::memset(&w, 0, sizeof(w));
+        w.depth = depth;
+        int32_t* ch = w.ch;
         int nch = 0;
-        if (n2[it.n2].count > 0) {
-            ch[nch++] = it.n2;                 // single-leaf root
+        if (n2[node2].count > 0) {
+            ch[nch++] = node2;                 // single-leaf root
         } else {
-            ch[nch++] = n2[it.n2].left;
-            ch[nch++] = n2[it.n2].right;
+            ch[nch++] = n2[node2].left;
+            ch[nch++] = n2[node2].right;
             while (nch < max_children) {
                 int best = -1;
                 float area = -1.f;
@@ -230,105 +305,154 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
                 ch[nch++] = n2[x].right;
             }
         }
-        // node box and slot assignment by octant
-        Box nb;
-        nb.reset();
-        for (int c = 0; c < nch; ++c) nb.grow(n2[ch[c]].box);
-        float pc[3];
-        for (int k = 0; k < 3; ++k) pc[k] = 0.5f * (nb.lo[k] + nb.hi[k]);
-        int slot_of[8];
-        bool used_slot[8] = {false}, placed[8] = {false};
-        for (int round = 0; round < nch; ++round) {
-            float best = -FLT_MAX;
-            int bc = -1, bs = -1;
-            for (int c = 0; c < nch; ++c) {
-                if (placed[c]) continue;
-                const Box& cb = n2[ch[c]].box;
-                float d[3];
-                for (int k = 0; k < 3; ++k) d[k] = 0.5f * (cb.lo[k] + cb.hi[k]) - pc[k];
-                for (int s = 0; s < 8; ++s) {
-                    if (used_slot[s]) continue;
-                    float sc = ((s & 1) ? d[0] : -d[0]) + ((s & 2) ? d[1] : -d[1]) + ((s & 4) ? d[2] : -d[2]);
-                    if (sc > best) { best = sc; bc = c; bs = s; }
-                }
+        w.nch = nch;
+        recs.push_back(w);
+    };
+    add_record(root, 1);
+    out.max_depth = 0;
+    for (size_t r = 0; r < recs.size(); ++r) {
+        const uint32_t depth = recs[r].depth;
+        out.max_depth = std::max(out.max_depth, depth);
+        if (depth > max_levels) { *msg = "BVH deeper than the traversal stack allows"; return false; }
+        for (int c = 0; c < recs[r].nch; ++c) {
+            const int32_t x = recs[r].ch[c];
+            if (n2[x].count == 0) {
+                recs[r].rec[c] = (int32_t)recs.size();
+                add_record(x, depth + 1);
+            } else {
+                recs[r].rec[c] = -1;
             }
-            placed[bc] = true;
-            used_slot[bs] = true;
-            slot_of[bc] = bs;
         }
+    }
+    parallel_for(recs.size(), [&](size_t r0, size_t r1) {
+        for (size_t r = r0; r < r1; ++r) {
+            Wide& w = recs[r];
+            Box nb;
+            nb.reset();
+            for (int c = 0; c < w.nch; ++c) nb.grow(n2[w.ch[c]].box);
+            float pc[3];
+            for (int k = 0; k < 3; ++k) pc[k] = 0.5f * (nb.lo[k] + nb.hi[k]);
+            bool used_slot[8] = {false}, placed[8] = {false};
+            for (int round = 0; round < w.nch; ++round) {
+                float best = -FLT_MAX;
+                int bc = -1, bs = -1;
+                for (int c = 0; c < w.nch; ++c) {
+                    if (placed[c]) continue;
+                    const Box& cb = n2[w.ch[c]].box;
+                    float d[3];
+                    for (int k = 0; k < 3; ++k) d[k] = 0.5f * (cb.lo[k] + cb.hi[k]) - pc[k];
+                    for (int s = 0; s < 8; ++s) {
+                        if (used_slot[s]) continue;
+                        float sc = ((s & 1) ? d[0] : -d[0]) + ((s & 2) ? d[1] : -d[1]) + ((s & 4) ? d[2] : -d[2]);
+                        if (sc > best) { best = sc; bc = c; bs = s; }
+                    }
+                }
+                placed[bc] = true;
+                used_slot[bs] = true;
+                w.slot_of[bc] = bs;
+            }
+        }
+    });
+    // breadth-first numbering in slot order
+    std::vector<int32_t> rec_at;                   // record of each wide node
+    rec_at.reserve(recs.size());
+    std::vector<uint32_t> child_base(recs.size()), tri_base(recs.size());
+    rec_at.push_back(0);
+    uint32_t tris_so_far = 0;
+    for (size_t q = 0; q < rec_at.size(); ++q) {
+        const Wide& w = recs[rec_at[q]];
         int child_at[8];
         for (int s = 0; s < 8; ++s) child_at[s] = -1;
-        for (int c = 0; c < nch; ++c) child_at[slot_of[c]] = ch[c];
-
-        Bvh8Node node;
-        std::memset(&node, 0, sizeof(node));
-        Bvh8FloatNode fnode;
-        std::memset(&fnode, 0, sizeof(fnode));
-        node.px = nb.lo[0];
-        node.py = nb.lo[1];
-        node.pz = nb.lo[2];
-        int e[3];
-        for (int k = 0; k < 3; ++k) e[k] = scale_exponent((double)nb.hi[k] - (double)nb.lo[k]);
-        node.ex = (uint8_t)(e[0] + 127);
-        node.ey = (uint8_t)(e[1] + 127);
-        node.ez = (uint8_t)(e[2] + 127);
-        node.child_base = (uint32_t)out.nodes.size();
-        node.tri_base = (uint32_t)out.tris.size();
-        uint32_t tri_off = 0;
+        for (int c = 0; c < w.nch; ++c) child_at[w.slot_of[c]] = c;
+        child_base[q] = (uint32_t)rec_at.size();
+        tri_base[q] = tris_so_far;
         for (int s = 0; s < 8; ++s) {
-            int32_t c = child_at[s];
-            if (c < 0) {
-                // empty slot: inverted box (lo plane above hi plane) never hits
-                for (int k = 0; k < 3; ++k) {
-                    node.qlo[k][s] = 255;
-                    node.qhi[k][s] = 0;
-                    fnode.lo[k][s] = FLT_MAX;
-                    fnode.hi[k][s] = -FLT_MAX;
-                }
-                continue;
-            }
-            const Node2& cn = n2[c];
-            for (int k = 0; k < 3; ++k) {
-                fnode.lo[k][s] = cn.box.lo[k];
-                fnode.hi[k][s] = cn.box.hi[k];
-            }
-            for (int k = 0; k < 3; ++k) {
-                double step = std::ldexp(1.0, e[k]);
-                double lo = std::floor(((double)cn.box.lo[k] - (double)nb.lo[k]) / step);
-                double hi = std::ceil(((double)cn.box.hi[k] - (double)nb.lo[k]) / step);
-                node.qlo[k][s] = (uint8_t)std::max(0.0, std::min(255.0, lo));
-                node.qhi[k][s] = (uint8_t)std::max(0.0, std::min(255.0, hi));
-            }
-            if (cn.count == 0) {
-                node.imask |= (uint8_t)(1u << s);
-                node.meta[s] = 0x80;
-                queue.push_back({c, it.depth + 1});
-            } else {
-                node.meta[s] = (uint8_t)((cn.count << 5) | tri_off);
-                for (uint32_t i = 0; i < cn.count; ++i) {
-                    uint32_t t = idx[cn.first + i];
-                    TriRecord r;
-                    for (int k = 0; k < 3; ++k) {
-                        r.v1[k] = v1[3 * t + k];
-                        r.e1[k] = e1[3 * t + k];
-                        r.e2[k] = e2[3 * t + k];
-                    }
-                    r.face = t;
-                    r.pad1 = r.pad2 = 0.f;
-                    out.tris.push_back(r);
-                }
-                tri_off += cn.count;
-            }
+            const int c = child_at[s];
+            if (c < 0) continue;
+            if (w.rec[c] >= 0) rec_at.push_back(w.rec[c]);
+            else tris_so_far += n2[w.ch[c]].count;
         }
-        out.nodes.resize(out.nodes.size() + __builtin_popcount(node.imask));
-        out.nodes[qi] = node;
-        if (node.child_base >= (1u << 24)) out.fnodes_ok = false;   // 24-bit child index
-        fnode.child_base_imask = node.child_base | ((uint32_t)node.imask << 24);
-        fnode.tri_base = node.tri_base;
-        std::memcpy(fnode.meta, node.meta, 8);
-        out.fnodes.resize(out.nodes.size());
-        out.fnodes[qi] = fnode;
     }
+    const size_t nn = rec_at.size();
+    out.nodes.assign(nn, Bvh8Node{});
+    out.fnodes.assign(nn, Bvh8FloatNode{});
+    out.tris.assign(tris_so_far, TriRecord{});
+    out.margin = margin;
+    out.fnodes_ok = nn == 0 || child_base[nn - 1] < (1u << 24);   // 24-bit child index
+    parallel_for(nn, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q) {
+            const Wide& w = recs[rec_at[q]];
+            int child_at[8];
+            for (int s = 0; s < 8; ++s) child_at[s] = -1;
+            for (int c = 0; c < w.nch; ++c) child_at[w.slot_of[c]] = c;
+            Box nb;
+            nb.reset();
+            for (int c = 0; c < w.nch; ++c) nb.grow(n2[w.ch[c]].box);
+            Bvh8Node node;
+            std::memset(&node, 0, sizeof(node));
+            Bvh8FloatNode fnode;
+            std::memset(&fnode, 0, sizeof(fnode));
+            node.px = nb.lo[0];
+            node.py = nb.lo[1];
+            node.pz = nb.lo[2];
+            int e[3];
+            for (int k = 0; k < 3; ++k) e[k] = scale_exponent((double)nb.hi[k] - (double)nb.lo[k]);
+            node.ex = (uint8_t)(e[0] + 127);
+            node.ey = (uint8_t)(e[1] + 127);
+            node.ez = (uint8_t)(e[2] + 127);
+            node.child_base = child_base[q];
+            node.tri_base = tri_base[q];
+            uint32_t tri_off = 0;
+            for (int s = 0; s < 8; ++s) {
+                const int c = child_at[s];
+                if (c < 0) {
+                    // empty slot: inverted box (lo plane above hi plane) never hits
+                    for (int k = 0; k < 3; ++k) {
+                        node.qlo[k][s] = 255;
+                        node.qhi[k][s] = 0;
+                        fnode.lo[k][s] = FLT_MAX;
+                        fnode.hi[k][s] = -FLT_MAX;
+                    }
+                    continue;
+                }
+                const Node2& cn = n2[w.ch[c]];
+                for (int k = 0; k < 3; ++k) {
+                    fnode.lo[k][s] = cn.box.lo[k];
+                    fnode.hi[k][s] = cn.box.hi[k];
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double step = std::ldexp(1.0, e[k]);
+                    double lo = std::floor(((double)cn.box.lo[k] - (double)nb.lo[k]) / step);
+                    double hi = std::ceil(((double)cn.box.hi[k] - (double)nb.lo[k]) / step);
+                    node.qlo[k][s] = (uint8_t)std::max(0.0, std::min(255.0, lo));
+                    node.qhi[k][s] = (uint8_t)std::max(0.0, std::min(255.0, hi));
+                }
+                if (w.rec[c] >= 0) {
+                    node.imask |= (uint8_t)(1u << s);
+                    node.meta[s] = 0x80;
+                } else {
+                    node.meta[s] = (uint8_t)((cn.count << 5) | tri_off);
+                    for (uint32_t i = 0; i < cn.count; ++i) {
+                        uint32_t t = idx[cn.first + i];
+                        TriRecord& r = out.tris[node.tri_base + tri_off + i];
+                        for (int k = 0; k < 3; ++k) {
+                            r.v1[k] = v1[3 * t + k];
+                            r.e1[k] = e1[3 * t + k];
+                            r.e2[k] = e2[3 * t + k];
+                        }
+                        r.face = t;
+                        r.pad1 = r.pad2 = 0.f;
+                    }
+                    tri_off += cn.count;
+                }
+            }
+            out.nodes[q] = node;
+            fnode.child_base_imask = node.child_base | ((uint32_t)node.imask << 24);
+            fnode.tri_base = node.tri_base;
+            std::memcpy(fnode.meta, node.meta, 8);
+            out.fnodes[q] = fnode;
+        }
+    });
     *msg = nullptr;
     return true;
 }

@@ -162,20 +162,28 @@ struct TraversalStats {
     uint32_t nodes, tris;
 };
 
+// Dynamic shared memory of the traversal kernels that stage the top of the
+// BVH: the first n_top nodes (BFS order: the shallowest levels, which every
+// ray visits) copied from HBM at kernel start, then the stacks.
+extern __shared__ float4 crt_top_nodes[];
+
 // Per-thread stack: shared-memory part (stride = threads per block) and a
-// local-memory overflow part.
+// local-memory overflow part.  It also carries how many top nodes the
+// launching kernel staged in shared memory (0: none).
 struct Stack {
     uint2* sh;           // this thread's first shared entry; entries are `stride` apart
     uint32_t stride;     // threads per block
     int depth;           // entries kept in shared memory
     int sp;
+    uint32_t n_top = 0;  // nodes [0, n_top) are in crt_top_nodes
     uint2 spill[kMaxLevels];
 
-    CRT_D void setup(uint2* base, uint32_t threads, int shared_depth) {
+    CRT_D void setup(uint2* base, uint32_t threads, int shared_depth, uint32_t staged_nodes = 0) {
         sh = base + threadIdx.x;
         stride = threads;
         depth = shared_depth;
         sp = 0;
+        n_top = staged_nodes;
     }
     CRT_D void push(uint2 e) {
         if (sp < depth) sh[sp * stride] = e;
@@ -304,11 +312,17 @@ struct Traversal {
 
     // Slab tests of the 8 children of an 80-byte node: planes are 8-bit
     // offsets from the node origin in units of a power-of-two scale.
-    CRT_D void test_children_q8(const DevScene& S, uint32_t node, uint32_t& child_base, uint32_t& child_imask,
-                                uint32_t& tri_base_new, uint32_t& meta_lo, uint32_t& meta_hi,
-                                uint32_t& hitmask) const {
-        const float4* np = S.nodes + 5ull * node;
-        const float4 n0 = ldg(np), n1 = ldg(np + 1), n2 = ldg(np + 2), n3 = ldg(np + 3), n4 = ldg(np + 4);
+    CRT_D void test_children_q8(const DevScene& S, uint32_t node, uint32_t n_top, uint32_t& child_base,
+                                uint32_t& child_imask, uint32_t& tri_base_new, uint32_t& meta_lo,
+                                uint32_t& meta_hi, uint32_t& hitmask) const {
+        float4 n0, n1, n2, n3, n4;
+        if (node < n_top) {
+            const float4* sp = crt_top_nodes + 5u * node;
+            n0 = sp[0]; n1 = sp[1]; n2 = sp[2]; n3 = sp[3]; n4 = sp[4];
+        } else {
+            const float4* np = S.nodes + 5ull * node;
+            n0 = ldg(np); n1 = ldg(np + 1); n2 = ldg(np + 2); n3 = ldg(np + 3); n4 = ldg(np + 4);
+        }
         const uint32_t ebits = __float_as_uint(n0.w);
         const float sx = __uint_as_float((ebits & 0xFFu) << 23) * ix;
         const float sy = __uint_as_float(((ebits >> 8) & 0xFFu) << 23) * iy;
@@ -347,11 +361,14 @@ struct Traversal {
 
     // Slab tests of the 8 children of a 208-byte node with FP32 planes:
     // t = plane * (1/d) - o * (1/d) in one fused multiply-add per plane.
-    CRT_D void test_children_f32(const DevScene& S, uint32_t node, uint32_t& child_base, uint32_t& child_imask,
-                                 uint32_t& tri_base_new, uint32_t& meta_lo, uint32_t& meta_hi,
-                                 uint32_t& hitmask) const {
+    CRT_D void test_children_f32(const DevScene& S, uint32_t node, uint32_t n_top, uint32_t& child_base,
+                                 uint32_t& child_imask, uint32_t& tri_base_new, uint32_t& meta_lo,
+                                 uint32_t& meta_hi, uint32_t& hitmask) const {
+        const bool staged = node < n_top;
         const float4* np = S.fnodes + 13ull * node;
-        const float4 hd = ldg(np + 12);
+        const float4* sp = crt_top_nodes + 13u * node;
+        auto load = [&](int i) { return staged ? sp[i] : ldg(np + i); };
+        const float4 hd = load(12);
         const uint32_t cbi = __float_as_uint(hd.x);
         child_base = cbi & 0xFFFFFFu;
         child_imask = cbi >> 24;
@@ -365,9 +382,9 @@ struct Traversal {
         hitmask = 0;
 #pragma unroll
         for (int half = 0; half < 2; ++half) {   // slots 4*half .. 4*half+3
-            const float4 nxv = ldg(np + nxo + half), fxv = ldg(np + (6 - nxo) + half);
-            const float4 nyv = ldg(np + nyo + half), fyv = ldg(np + (10 - nyo) + half);
-            const float4 nzv = ldg(np + nzo + half), fzv = ldg(np + (14 - nzo) + half);
+            const float4 nxv = load(nxo + half), fxv = load((6 - nxo) + half);
+            const float4 nyv = load(nyo + half), fyv = load((10 - nyo) + half);
+            const float4 nzv = load(nzo + half), fzv = load((14 - nzo) + half);
             const float nxs[4] = {nxv.x, nxv.y, nxv.z, nxv.w}, fxs[4] = {fxv.x, fxv.y, fxv.z, fxv.w};
             const float nys[4] = {nyv.x, nyv.y, nyv.z, nyv.w}, fys[4] = {fyv.x, fyv.y, fyv.z, fyv.w};
             const float nzs[4] = {nzv.x, nzv.y, nzv.z, nzv.w}, fzs[4] = {fzv.x, fzv.y, fzv.z, fzv.w};
@@ -402,8 +419,8 @@ struct Traversal {
         if (COUNT) stats->nodes++;
 
         uint32_t child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask;
-        if (F32) test_children_f32(S, node, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);
-        else test_children_q8(S, node, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);
+        if (F32) test_children_f32(S, node, st.n_top, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);
+        else test_children_q8(S, node, st.n_top, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);
         // Empty slots hold inverted boxes and never hit; a leaf's meta byte
         // gives its triangle count (bits 5-6) and offset (bits 0-4).
         uint32_t leaves = hitmask & ~child_imask;

@@ -51,6 +51,7 @@ struct crt_scene_s {
     crt::DevScene dev{};            // both node encodings uploaded
     bool default_f32 = false;       // encoding renders use unless told otherwise
     uint32_t n_mats = 0;
+    bool ka_scaled = false;         // materials were given with the emission scaling applied
     uint32_t generation = 0;        // bumped whenever the BVH buffers are replaced
     crt_scene_info info{};
 
@@ -68,7 +69,7 @@ struct WaveBuffers {
     uint32_t capacity = 0;
     uint32_t seg_capacity = 0;      // wave segments the segs buffer holds
     crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, counters, waves, segs, prof;
-    crt::DevBuf adj_L, adj_W, adj_shadow;   // adjoint replay state, allocated on first use
+    crt::DevBuf adj_L, adj_W, adj_shadow, adj_hist;   // adjoint replay state, allocated on first use
 };
 
 // One independent set of wavefront buffers with its own stream and captured
@@ -80,6 +81,7 @@ struct WaveSet {
     void* graph = nullptr;
     void* adj_graph = nullptr;        // adjoint wave body, captured for adj_key's pointers
     const void* adj_key[3] = {nullptr, nullptr, nullptr};
+    uint32_t adj_flags = 0;
 };
 
 namespace crt {
@@ -95,8 +97,10 @@ struct ViewState {
     uint32_t spp = 0;               // samples per pixel one batch render adds
     uint32_t view_id = 0;           // Philox counter word
     uint32_t pix_off = 0;
-    uint32_t samples_rendered = 0;
+    uint32_t first_sample = 0;      // sample index the accumulator starts at
+    uint32_t samples_rendered = 0;  // samples in the accumulator
     uint32_t npix() const { return width * height; }
+    uint32_t next_sample() const { return first_sample + samples_rendered; }
 };
 
 // Samples [spp0, spp0 + nspp) of one view, rendered by a pass.
@@ -110,7 +114,7 @@ struct crt_render_s {
     crt_render_options opts{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    crt::DevBuf accum, lut, ray_counts, view_table;
+    crt::DevBuf accum, lut, ray_counts, view_table, staging;
     std::vector<WaveSet> sets;
     uint32_t scene_generation = 0;  // scene BVH the captured wave graphs point at
     cudaEvent_t pass_start = nullptr;
@@ -130,6 +134,10 @@ inline bool uses_f32_nodes(const crt_render_s* r) { return uses_f32_nodes(r->sce
 inline uint32_t traversal_block(const crt_render_options& o) { return o.block_size ? o.block_size : 128u; }
 inline uint32_t traversal_stack(const crt_render_options& o) { return o.stack_depth ? o.stack_depth : 16u; }
 inline uint32_t queue_chunk(const crt_render_options& o) { return o.queue_chunk ? o.queue_chunk : 32u; }
+inline uint32_t refill_busy(const crt_render_options& o) { return o.refill_busy ? o.refill_busy : 31u; }
+inline uint32_t staged_nodes(const crt_scene_s* s, const crt_render_options& o) {
+    return o.top_nodes < s->info.num_nodes ? o.top_nodes : s->info.num_nodes;
+}
 
 // Checks the fields every render entry point shares; CRT_OK or an error.
 inline int check_render_options(const crt_render_options& o) {
@@ -144,6 +152,8 @@ inline int check_render_options(const crt_render_options& o) {
     if (o.queue_chunk != 0 && o.queue_chunk != 32 && o.queue_chunk != 64 && o.queue_chunk != 128 &&
         o.queue_chunk != 256)
         return set_error(CRT_ERR_INVALID, "queue_chunk must be 0, 32, 64, 128 or 256");
+    if (o.top_nodes > 128) return set_error(CRT_ERR_INVALID, "top_nodes must be in [0, 128]");
+    if (o.refill_busy > 31) return set_error(CRT_ERR_INVALID, "refill_busy must be in [0, 31]");
     return CRT_OK;
 }
 

@@ -14,7 +14,8 @@ namespace crt {
 int grid_for(uint32_t n, int block, int per_sm);
 int wavefront_pass(crt_render r, const std::vector<ViewWork>& work);
 int wavefront_profile_pass(crt_render r, const std::vector<ViewWork>& work, crt_stage_profile* out);
-int wavefront_adjoint(crt_render r, const std::vector<ViewWork>& work, const float4* adj, float* gkd, float* gka);
+int wavefront_adjoint(crt_render r, const std::vector<ViewWork>& work, const float4* adj, float* gkd, float* gka,
+                      uint32_t flags);
 
 constexpr int kMegaBlock = 128;         // 16 x 8 pixel tile, warps of 8 x 4
 constexpr uint32_t kMegaSppPerLaunch = 4;
@@ -59,6 +60,18 @@ __global__ void resolve_kernel(const float4* __restrict__ accum, uint32_t n, flo
         const uint32_t qy = (uint32_t)((vy > 1.0f ? 1.0f : vy) * 255.f);
         const uint32_t qz = (uint32_t)((vz > 1.0f ? 1.0f : vz) * 255.f);
         out[i] = make_uchar4(L[qx & 255u], L[qy & 255u], L[qz & 255u], 255u);
+    }
+}
+
+// renderKernel's device-side image: float3ToUchar4 of the average, no gamma.
+__global__ void average_u8_kernel(const float4* __restrict__ accum, uint32_t n, float spp,
+                                  uchar4* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = accum[i];
+        const float vx = a.x / spp, vy = a.y / spp, vz = a.z / spp;
+        out[i] = make_uchar4((unsigned char)((vx > 1.0f ? 1.0f : vx) * 255.f),
+                             (unsigned char)((vy > 1.0f ? 1.0f : vy) * 255.f),
+                             (unsigned char)((vz > 1.0f ? 1.0f : vz) * 255.f), 255u);
     }
 }
 
@@ -209,7 +222,7 @@ static int run_pass(crt_render r, const std::vector<ViewWork>& work, crt_stage_p
 
 static std::vector<ViewWork> uniform_work(crt_render r, uint32_t n_spp) {
     std::vector<ViewWork> w;
-    for (const ViewState& V : r->views) w.push_back({V.samples_rendered, n_spp});
+    for (const ViewState& V : r->views) w.push_back({V.next_sample(), n_spp});
     return w;
 }
 
@@ -324,7 +337,7 @@ int crt_render_pass(crt_render r, uint32_t n_spp) {
 int crt_batch_render(crt_render r) {
     if (!r) return set_error(CRT_ERR_INVALID, "null render");
     std::vector<ViewWork> w;
-    for (const ViewState& V : r->views) w.push_back({V.samples_rendered, V.spp});
+    for (const ViewState& V : r->views) w.push_back({V.next_sample(), V.spp});
     return run_pass(r, w, nullptr);
 }
 
@@ -338,13 +351,14 @@ int crt_render_profile_pass(crt_render r, uint32_t n_spp, crt_stage_profile* out
 }
 
 int crt_render_adjoint(crt_render r, uint32_t spp0, uint32_t n_spp, const float* d_adjoint, float* d_grad_kd,
-                       float* d_grad_ka) {
+                       float* d_grad_ka, uint32_t flags) {
     if (!r || !d_adjoint || !d_grad_kd || !d_grad_ka) return set_error(CRT_ERR_INVALID, "crt_render_adjoint: null argument");
     if (((uintptr_t)d_adjoint & 15u) != 0) return set_error(CRT_ERR_INVALID, "d_adjoint must be 16-byte aligned");
     if (n_spp == 0) return CRT_OK;
     if ((uint64_t)spp0 + n_spp >= (1ull << 32)) return set_error(CRT_ERR_LIMIT, "sample index overflow");
     std::vector<ViewWork> work(r->views.size(), ViewWork{spp0, n_spp});
-    return wavefront_adjoint(r, work, reinterpret_cast<const float4*>(d_adjoint), d_grad_kd, d_grad_ka);
+    if (flags & ~(uint32_t)CRT_ADJOINT_EXACT_ROULETTE) return set_error(CRT_ERR_INVALID, "unknown adjoint flag");
+    return wavefront_adjoint(r, work, reinterpret_cast<const float4*>(d_adjoint), d_grad_kd, d_grad_ka, flags);
 }
 
 int crt_render_samples_rendered(crt_render r, uint32_t* out) {
@@ -387,6 +401,54 @@ int crt_render_view_resolve(crt_render r, uint32_t view, uint8_t* host_rgba) {
     return resolve_view(r, view, host_rgba);
 }
 
+int crt_render_resolve_device(crt_render r, void* d_rgba) {
+    if (!r || !d_rgba) return set_error(CRT_ERR_INVALID, "null argument");
+    const ViewState& V = r->views[0];
+    if (V.samples_rendered == 0) return set_error(CRT_ERR_INVALID, "no samples rendered");
+    const uint32_t n = V.npix();
+    average_u8_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>() + V.pix_off, n,
+                                                                 (float)V.samples_rendered, (uchar4*)d_rgba);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}
+
+int crt_render_resolve_async(crt_render r, uint8_t* host_rgba) {
+    if (!r || !host_rgba) return set_error(CRT_ERR_INVALID, "null argument");
+    const ViewState& V = r->views[0];
+    if (V.samples_rendered == 0) return set_error(CRT_ERR_INVALID, "no samples rendered");
+    const uint32_t n = V.npix();
+    if (r->staging.bytes < (size_t)n * 4) CRT_CUDA(r->staging.alloc((size_t)n * 4));
+    resolve_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(r->accum.as<float4>() + V.pix_off, n,
+                                                              (float)V.samples_rendered,
+                                                              r->lut.as<uint8_t>(), r->staging.as<uchar4>());
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaMemcpyAsync(host_rgba, r->staging.p, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
+    return CRT_OK;
+}
+
+__global__ void pack_accum_kernel(const float* __restrict__ in, uint32_t n, float4* __restrict__ accum) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        accum[i] = make_float4(in[3ull * i], in[3ull * i + 1], in[3ull * i + 2], 0.f);
+}
+
+int crt_render_load_accum(crt_render r, uint32_t view, const float* host_rgb, uint32_t samples,
+                          uint32_t first_sample) {
+    if (!r || !host_rgb) return set_error(CRT_ERR_INVALID, "null argument");
+    if (view >= r->views.size()) return set_error(CRT_ERR_INVALID, "view index out of range");
+    if ((uint64_t)first_sample + samples >= (1ull << 32)) return set_error(CRT_ERR_LIMIT, "sample index overflow");
+    ViewState& V = r->views[view];
+    const uint32_t n = V.npix();
+    DevBuf tmp;
+    CRT_CUDA(tmp.alloc((size_t)n * 12));
+    CRT_CUDA(cudaMemcpyAsync(tmp.p, host_rgb, (size_t)n * 12, cudaMemcpyHostToDevice, r->stream));
+    pack_accum_kernel<<<grid_for(n, 256, 8), 256, 0, r->stream>>>(tmp.as<float>(), n, r->accum.as<float4>() + V.pix_off);
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaStreamSynchronize(r->stream));
+    V.first_sample = first_sample;
+    V.samples_rendered = samples;
+    return CRT_OK;
+}
+
 int crt_render_accum(crt_render r, float* host_rgb) {
     if (!r || !host_rgb) return set_error(CRT_ERR_INVALID, "null argument");
     return accum_view(r, 0, host_rgb);
@@ -408,7 +470,18 @@ int crt_render_reset(crt_render r) {
     if (!r) return set_error(CRT_ERR_INVALID, "null render");
     CRT_CUDA(cudaMemsetAsync(r->accum.p, 0, r->accum.bytes, r->stream));
     CRT_CUDA(cudaMemsetAsync(r->ray_counts.p, 0, r->ray_counts.bytes, r->stream));
-    for (ViewState& V : r->views) V.samples_rendered = 0;
+    for (ViewState& V : r->views) V.first_sample = V.samples_rendered = 0;
+    return CRT_OK;
+}
+
+int crt_render_restart(crt_render r, uint32_t first_sample) {
+    if (!r) return set_error(CRT_ERR_INVALID, "null render");
+    CRT_CUDA(cudaMemsetAsync(r->accum.p, 0, r->accum.bytes, r->stream));
+    CRT_CUDA(cudaMemsetAsync(r->ray_counts.p, 0, r->ray_counts.bytes, r->stream));
+    for (ViewState& V : r->views) {
+        V.first_sample = first_sample;
+        V.samples_rendered = 0;
+    }
     return CRT_OK;
 }
 

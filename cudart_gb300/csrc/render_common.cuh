@@ -63,11 +63,15 @@ struct ShadowReq {
 // * albedo(m, kd, color): a diffuse vertex of untextured material m is about
 //   to multiply the throughput by kd; everything the path adds from here on
 //   (its total minus `color`, the radiance so far) carries one factor kd.
-// Russian roulette's survival probability is treated as a constant.
+// * roulette(mask, color): the path survived Russian roulette and is about
+//   to divide its throughput by max_component(mask).  By default the
+//   survival probability counts as a constant (the hook does nothing); the
+//   exact mode differentiates that division as well.
 struct NoGrad {
     static constexpr bool kActive = false;
     CRT_D void emission(uint32_t, float3) {}
     CRT_D void albedo(uint32_t, float3, float3) {}
+    CRT_D void roulette(float3, float3) {}
 };
 
 CRT_D void begin_path(const Camera& cam, uint64_t seed, uint32_t view, uint32_t x, uint32_t y, uint32_t pixel,
@@ -176,6 +180,7 @@ CRT_D bool shade_hit(const RenderParams& P, PathState& ps, Ray& ray, const Hit& 
     if (b >= 3) {
         const float p = max_component(ps.mask);
         if (ps.rng.next() > p) return false;
+        if (G::kActive) g->roulette(ps.mask, ps.color);
         ps.mask = ps.mask / p;
     }
     return true;

@@ -70,6 +70,23 @@ inline float4 f4(float x, float y, float z, float w) { return make_float4(x, y, 
 inline float bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline float bits(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
 
+// Materials (createMaterialsData, parallel_renderer.cu:252-279) with the
+// emission scaling ka = Ka * 3 * lightsArea (scene.cpp:163,177).
+static std::vector<float4> pack_materials(const crt_material* ms, uint32_t n, float lights_area,
+                                          bool ka_scaled) {
+    std::vector<float4> mats(4ull * n);
+    for (uint32_t m = 0; m < n; ++m) {
+        const crt_material& M = ms[m];
+        float ka[3];
+        for (int k = 0; k < 3; ++k) ka[k] = ka_scaled ? M.ka[k] : (M.ka[k] * 3.0f) * lights_area;
+        mats[4 * m + 0] = f4(M.kd[0], M.kd[1], M.kd[2], bits((int32_t)M.texture));
+        mats[4 * m + 1] = f4(ka[0], ka[1], ka[2], bits((int32_t)M.bsdf));
+        mats[4 * m + 2] = f4(M.ks[0], M.ks[1], M.ks[2], M.ns);
+        mats[4 * m + 3] = f4(M.ni, M.diffuse, 0.f, 0.f);
+    }
+    return mats;
+}
+
 }  // namespace
 }  // namespace crt
 
@@ -130,6 +147,8 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     if (d->num_textures && (!d->texture_dims || !d->texels))
         return set_error(CRT_ERR_INVALID, "textures need dims and texels");
     if (d->node_format > CRT_NODES_F32) return set_error(CRT_ERR_INVALID, "unknown node format");
+    if (d->flags & ~(uint32_t)(CRT_SCENE_EDGES | CRT_SCENE_KA_SCALED))
+        return set_error(CRT_ERR_INVALID, "unknown scene flag");
     if (d->bvh_width != 0 && d->bvh_width != 4 && d->bvh_width != 8)
         return set_error(CRT_ERR_INVALID, "bvh_width must be 4 or 8");
 
@@ -137,13 +156,14 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     crt_scene s = new crt_scene_s();
 
     // Triangle geometry as Scene::loadTriangles computes it (scene.cpp:111-130).
+    const bool edges = (d->flags & CRT_SCENE_EDGES) != 0;
     std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n), area(n);
     for (uint32_t i = 0; i < n; ++i) {
         const float* p = d->positions + 9ull * i;
         for (int k = 0; k < 3; ++k) {
             v1[3 * i + k] = p[k];
-            e1[3 * i + k] = p[3 + k] - p[k];
-            e2[3 * i + k] = p[6 + k] - p[k];
+            e1[3 * i + k] = edges ? p[3 + k] : p[3 + k] - p[k];
+            e2[3 * i + k] = edges ? p[6 + k] : p[6 + k] - p[k];
         }
         const float* a = &e1[3 * i];
         const float* b = &e2[3 * i];
@@ -194,18 +214,8 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
             uvs[2 * i + 0] = uvs[2 * i + 1] = f4(0.f, 0.f, 0.f, 0.f);
         }
     }
-    // Materials (createMaterialsData, parallel_renderer.cu:252-279) with the
-    // emission scaling ka = Ka * 3 * lightsArea (scene.cpp:163,177).
-    std::vector<float4> mats(4ull * d->num_materials);
-    for (uint32_t m = 0; m < d->num_materials; ++m) {
-        const crt_material& M = d->materials[m];
-        float ka[3];
-        for (int k = 0; k < 3; ++k) ka[k] = (M.ka[k] * 3.0f) * lights_area;
-        mats[4 * m + 0] = f4(M.kd[0], M.kd[1], M.kd[2], bits((int32_t)M.texture));
-        mats[4 * m + 1] = f4(ka[0], ka[1], ka[2], bits((int32_t)M.bsdf));
-        mats[4 * m + 2] = f4(M.ks[0], M.ks[1], M.ks[2], M.ns);
-        mats[4 * m + 3] = f4(M.ni, M.diffuse, 0.f, 0.f);
-    }
+    const std::vector<float4> mats =
+        pack_materials(d->materials, d->num_materials, lights_area, (d->flags & CRT_SCENE_KA_SCALED) != 0);
     std::vector<float4> lgeo(3 * s->lights.size());
     for (size_t i = 0; i < s->lights.size(); ++i) {
         uint32_t f = s->lights[i];
@@ -243,6 +253,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     // fit 24 bits); each render picks one.
     s->default_f32 = f32;
     s->n_mats = d->num_materials;
+    s->ka_scaled = (d->flags & CRT_SCENE_KA_SCALED) != 0;
     if ((st = install_bvh(s, bvh, width)) ||
         (st = upload(s->shade, shade)) || (st = upload(s->uvs, uvs)) || (st = upload(s->mats, mats)) ||
         (st = upload(s->light_geo, lgeo)) || (st = upload(s->texels, texels)) ||
@@ -283,6 +294,23 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
 int crt_scene_destroy(crt_scene s) {
     delete s;
+    return CRT_OK;
+}
+
+int crt_scene_set_materials(crt_scene s, const crt_material* materials, uint32_t n) {
+    if (!s || !materials) return set_error(CRT_ERR_INVALID, "crt_scene_set_materials: null argument");
+    if (n != s->n_mats) return set_error(CRT_ERR_INVALID, "crt_scene_set_materials: material count differs");
+    for (uint32_t m = 0; m < n; ++m) {
+        const int t = materials[m].texture;
+        if (t != CRT_NO_TEXTURE && (t < 0 || (uint32_t)t >= s->info.num_textures))
+            return set_error(CRT_ERR_INVALID, "texture index out of range in material " + std::to_string(m));
+        if (materials[m].bsdf < 0 || materials[m].bsdf > CRT_BSDF_EMISSIVE)
+            return set_error(CRT_ERR_INVALID, "unknown bsdf in material " + std::to_string(m));
+    }
+    const std::vector<float4> mats = pack_materials(materials, n, s->info.lights_area, s->ka_scaled);
+    CRT_CUDA(cudaSetDevice(s->device));
+    CRT_CUDA(cudaDeviceSynchronize());   // no queued pass may read a half-written table
+    CRT_CUDA(cudaMemcpy(s->mats.p, mats.data(), mats.size() * sizeof(float4), cudaMemcpyHostToDevice));
     return CRT_OK;
 }
 

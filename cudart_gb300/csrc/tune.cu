@@ -5,7 +5,8 @@
 // thread per pixel, renderer.cu:543-551) and has nothing to tune.  Here the
 // options that change speed but never the image -- node encoding, traversal
 // block size, shared-memory stack depth, queue entries claimed per fetch,
-// wave sets in flight, paths per wave, lane refill, and the BVH's width --
+// wave sets in flight, paths per wave, lane refill and its threshold, top BVH
+// nodes staged in shared memory, and the BVH's width --
 // are searched by coordinate descent: each axis in turn is swept with the
 // others held, and a value is adopted when it beats the current best by more
 // than the noise margin.  Every candidate renders the same samples (a fresh
@@ -24,11 +25,12 @@ namespace {
 
 constexpr float kAdoptMargin = 0.02f;   // a candidate must be 2 % faster to move the search
 
-using Key = std::tuple<int32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t>;
+using Key = std::tuple<int32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
+                       uint32_t>;
 
 Key key_of(const crt_render_options& o, uint32_t bvh_width) {
     return Key(o.node_format, o.block_size, o.stack_depth, o.queue_chunk, o.wave_sets, o.wave_paths,
-               o.flags, bvh_width);
+               o.flags, o.top_nodes, o.refill_busy, bvh_width);
 }
 
 struct Tuner {
@@ -114,7 +116,7 @@ struct Tuner {
             {&crt_render_options::wave_sets, {1, 2, 3, 4}},
             {&crt_render_options::wave_paths, {1u << 20, 1u << 21, 1u << 22}},
             {&crt_render_options::queue_chunk, {32, 64, 128}},
-            {&crt_render_options::flags, {0u, (uint32_t)CRT_FLAG_LANE_REFILL}},
+            {&crt_render_options::top_nodes, {0, 9, 73}},
         };
         for (const Axis& a : axes) {
             for (uint32_t v : a.values) {
@@ -126,6 +128,21 @@ struct Tuner {
                     cur = c;
                     t = tc;
                 }
+            }
+        }
+        // scheduling: batch fetch, or lane refill at a busy-lane threshold
+        const uint32_t sched[][2] = {{0u, 31u}, {CRT_FLAG_LANE_REFILL, 31u}, {CRT_FLAG_LANE_REFILL, 20u},
+                                     {CRT_FLAG_LANE_REFILL, 12u}};
+        for (const auto& sv : sched) {
+            const uint32_t flags = (cur.flags & ~(uint32_t)CRT_FLAG_LANE_REFILL) | sv[0];
+            if (flags == cur.flags && sv[1] == cur.refill_busy) continue;
+            crt_render_options c = cur;
+            c.flags = flags;
+            c.refill_busy = sv[1];
+            const float tc = measure(c);
+            if (tc > 0.f && tc < t * (1.f - kAdoptMargin)) {
+                cur = c;
+                t = tc;
             }
         }
         return t;
@@ -150,6 +167,7 @@ crt_render_options explicit_options(const crt_render_options& in, const crt_scen
     o.block_size = traversal_block(o);
     o.stack_depth = traversal_stack(o);
     o.queue_chunk = queue_chunk(o);
+    o.refill_busy = refill_busy(o);
     if (!o.wave_sets) o.wave_sets = 3;
     if (!o.wave_paths) o.wave_paths = 1u << 22;
     o.node_format = uses_f32_nodes(s, o.node_format) ? CRT_NODES_F32 : CRT_NODES_Q8;

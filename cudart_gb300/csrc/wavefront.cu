@@ -36,6 +36,9 @@ RenderParams make_params(crt_render r, uint32_t view, uint32_t spp0, uint32_t ns
 
 constexpr int kWaveBlock = 128;            // generate / shade / counting kernels
 constexpr int kTraversalBlockMax = 256;    // extend / shadow: block size chosen at launch
+#ifndef CRT_TRAVERSAL_MIN_BLOCKS
+#define CRT_TRAVERSAL_MIN_BLOCKS 1             // resident 256-thread blocks the register budget must allow
+#endif
 constexpr uint32_t kDefaultCapacity = 1u << 22;
 constexpr uint32_t kDefaultWaveSets = 3;
 constexpr uint32_t kMaxWaves = 1u << 16;   // descriptors uploaded per chunk
@@ -81,6 +84,8 @@ struct WaveParams {
     unsigned long long* prof;   // ProfileCounter totals (profiling pass only)
     int stack_depth;            // traversal stack entries in shared memory
     uint32_t queue_chunk;       // queue entries a warp claims per fetch (batch mode)
+    uint32_t top_nodes;         // BVH nodes staged in shared memory by extend / shadow
+    uint32_t refill_busy;       // lane refill: busy lanes at or below which idle lanes refill
     // adjoint replay only
     const float4* adj;          // d(objective)/d(radiance sum), per pixel of every view
     float4* st_L;               // radiance of each path's primal trace
@@ -89,7 +94,21 @@ struct WaveParams {
     float* grad_kd;             // [n_mats][3], added to
     float* grad_ka;             // [n_mats][3], added to
     uint32_t n_mats;
+    uint16_t* adj_hist;         // exact roulette: [capacity][kHistMax] kd-factor materials
+    bool adj_exact;
 };
+
+// Exact-roulette bookkeeping per path, kept in st_W.w: history length
+// (bits 0-4); history length and channel at the previous applied roulette
+// (5-9, 10-11); a surviving roulette not yet applied (flag 19) with its
+// history length and channel (12-16, 17-18).
+constexpr uint32_t kHistMax = 16;
+CRT_D uint32_t hist_len(uint32_t meta) { return meta & 31u; }
+CRT_D uint32_t hist_prev_len(uint32_t meta) { return (meta >> 5) & 31u; }
+CRT_D uint32_t hist_prev_channel(uint32_t meta) { return (meta >> 10) & 3u; }
+CRT_D uint32_t hist_pend_len(uint32_t meta) { return (meta >> 12) & 31u; }
+CRT_D uint32_t hist_pend_channel(uint32_t meta) { return (meta >> 17) & 3u; }
+constexpr uint32_t kHistPending = 1u << 19;
 
 // ---------------------------------------------------------------------------
 // Adjoint (path-replay backpropagation) helpers.  Gradients are summed per
@@ -131,18 +150,62 @@ CRT_D void flush_grad_block(const WaveParams& W, const float* acc) {
     }
 }
 
+CRT_D float channel(float3 v, uint32_t c) { return c == 0 ? v.x : c == 1 ? v.y : v.z; }
+CRT_D float3 in_channel(uint32_t c, float x) { return f3(c == 0 ? x : 0.f, c == 1 ? x : 0.f, c == 2 ? x : 0.f); }
+
 // The shade_hit hooks of the replay (see NoGrad): w is the adjoint weight of
 // the path's pixel, total the radiance its primal trace returned.
 struct WaveGrad {
     static constexpr bool kActive = true;
     float* acc;
     float3 w, total;
+    const DevScene* S = nullptr;   // exact roulette only: kd of history entries
+    uint16_t* hist = nullptr;      // this path's history, or null (constant survival probability)
+    uint32_t meta = 0;
     CRT_D void emission(uint32_t m, float3 d) { warp_add_grad(acc, m, 3, w * d); }
     CRT_D void albedo(uint32_t m, float3 kd, float3 color) {
         const float3 rest = total - color;
         const float3 g = f3(kd.x != 0.f ? w.x * rest.x / kd.x : 0.f, kd.y != 0.f ? w.y * rest.y / kd.y : 0.f,
                             kd.z != 0.f ? w.z * rest.z / kd.z : 0.f);
         warp_add_grad(acc, m, 0, g);
+        if (hist && hist_len(meta) < kHistMax) {
+            hist[hist_len(meta)] = (uint16_t)m;
+            ++meta;
+        }
+    }
+    // After a surviving roulette the throughput is mask / mask[c] (c the
+    // channel max_component picks): every later term gets -1/kd[c] per kd
+    // factor so far, in channel c, replacing the previous roulette's
+    // correction.  "Later" starts after this vertex's light sample, which the
+    // shadow kernel adds after shade, so the correction is recorded here and
+    // applied at the path's next shade (a path that ends first adds nothing
+    // later, and its correction is zero).
+    CRT_D void roulette(float3 mask, float3) {
+        if (!hist) return;
+        const uint32_t c01 = mask.x > mask.y ? 0u : 1u;
+        const float v01 = mask.x > mask.y ? mask.x : mask.y;
+        const uint32_t c = v01 > mask.z ? c01 : 2u;
+        meta = (meta & 0xFFFu) | (hist_len(meta) << 12) | (c << 17) | kHistPending;
+    }
+    // The pending roulette correction, with `color` the radiance the path
+    // had gathered by the end of that roulette's vertex.
+    CRT_D void apply_pending(float3 color) {
+        if (!hist || !(meta & kHistPending)) return;
+        const float3 rest = total - color;
+        const float s = w.x * rest.x + w.y * rest.y + w.z * rest.z;
+        const uint32_t n = hist_pend_len(meta), c = hist_pend_channel(meta);
+        const uint32_t pn = hist_prev_len(meta), pc = hist_prev_channel(meta);
+        for (uint32_t i = 0; i < n; ++i) {
+            const uint32_t m = hist[i];
+            const float k = channel(load_material(*S, m).kd, c);
+            warp_add_grad(acc, m, 0, in_channel(c, k != 0.f ? -s / k : 0.f));
+        }
+        for (uint32_t i = 0; i < pn; ++i) {
+            const uint32_t m = hist[i];
+            const float k = channel(load_material(*S, m).kd, pc);
+            warp_add_grad(acc, m, 0, in_channel(pc, k != 0.f ? s / k : 0.f));
+        }
+        meta = hist_len(meta) | (n << 5) | (c << 10);
     }
 };
 
@@ -197,7 +260,9 @@ __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
         const DevView& V = W.views[sg.view];
         if (REPLAY) {
             W.st_L[i] = W.st_c[i];
-            W.st_W[i] = W.adj[V.pix_off + pixel];
+            float4 a = W.adj[V.pix_off + pixel];
+            a.w = __uint_as_float(0u);   // exact-roulette history: empty
+            W.st_W[i] = a;
         }
         PathState ps;
         Ray ray;
@@ -221,18 +286,22 @@ __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
 // start(i) (initialise the lane's traversal for queue entry i), step() and
 // finish().
 template <bool REFILL, class Job>
-CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, uint32_t chunk, Job& job) {
+CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, uint32_t chunk, uint32_t refill_busy, Job& job) {
     if (REFILL) {
+        // idle lanes take new entries together, once at most `refill_busy`
+        // lanes of the warp are still busy (31: as soon as one is idle)
         bool active = false;
         WarpPool pool;
         pool.init();
         for (;;) {
-            const uint32_t i = pool.take(!active, fetch, n);
-            if (i != UINT32_MAX) {
-                job.start(i);
-                active = true;
+            if ((uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, active)) <= refill_busy) {
+                const uint32_t i = pool.take(!active, fetch, n);
+                if (i != UINT32_MAX) {
+                    job.start(i);
+                    active = true;
+                }
+                if (!__any_sync(0xFFFFFFFFu, active)) break;
             }
-            if (!__any_sync(0xFFFFFFFFu, active)) break;
             if (active && job.step()) {
                 job.finish();
                 active = false;
@@ -277,14 +346,26 @@ struct ExtendJob {
     }
 };
 
-template <bool REFILL, bool WHOLE_LEAF, bool F32>
-__global__ void __launch_bounds__(kTraversalBlockMax) wf_extend(WaveParams W) {
-    extern __shared__ uint2 stack_dyn[];
+// Copies the first W.top_nodes nodes to the start of dynamic shared memory
+// and returns where the stacks begin (TOP = false: no staging at all).
+template <bool F32, bool TOP>
+CRT_D uint2* stage_top_nodes(const WaveParams& W) {
+    if (!TOP) return reinterpret_cast<uint2*>(crt_top_nodes);
+    const uint32_t n = W.top_nodes * (F32 ? 13u : 5u);
+    const float4* src = F32 ? W.R.S.fnodes : W.R.S.nodes;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) crt_top_nodes[i] = ldg(src + i);
+    __syncthreads();
+    return reinterpret_cast<uint2*>(crt_top_nodes + n);
+}
+
+template <bool REFILL, bool WHOLE_LEAF, bool F32, bool TOP>
+__global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) wf_extend(WaveParams W) {
+    uint2* stacks = stage_top_nodes<F32, TOP>(W);
     Stack st;
-    st.setup(stack_dyn, blockDim.x, W.stack_depth);
+    st.setup(stacks, blockDim.x, W.stack_depth, TOP ? W.top_nodes : 0u);
     const uint32_t cur = W.counters[C_CUR];
     ExtendJob<WHOLE_LEAF, F32> job(W, W.queue[cur], st);
-    persistent_loop<REFILL>(W.counters[cur], &W.counters[C_FETCH_EXT], W.queue_chunk, job);
+    persistent_loop<REFILL>(W.counters[cur], &W.counters[C_FETCH_EXT], W.queue_chunk, W.refill_busy, job);
     count_rays(W.R.ray_counts, job.rays, 0);
 }
 
@@ -325,12 +406,24 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
             h.face = __float_as_int(hv.y);
             h.u = hv.z;
             h.v = hv.w;
-            if (h.face < 0) {
+            if (ADJ) {
+                const float4 wv = W.st_W[path];
+                WaveGrad g{grad_sh, xyz(wv), xyz(W.st_L[path])};
+                if (W.adj_exact) {
+                    g.S = &W.R.S;
+                    g.hist = W.adj_hist + (size_t)path * kHistMax;
+                    g.meta = __float_as_uint(wv.w);
+                    g.apply_pending(ps.color);
+                }
+                if (h.face < 0) {
+                    shade_miss(ps);
+                } else {
+                    alive = shade_hit(W.R, ps, ray, h, sr, &g) && ps.bounce < W.R.max_depth;
+                    want_shadow = sr.valid;
+                }
+                if (W.adj_exact) W.st_W[path].w = __uint_as_float(g.meta);
+            } else if (h.face < 0) {
                 shade_miss(ps);
-            } else if (ADJ) {
-                WaveGrad g{grad_sh, xyz(W.st_W[path]), xyz(W.st_L[path])};
-                alive = shade_hit(W.R, ps, ray, h, sr, &g) && ps.bounce < W.R.max_depth;
-                want_shadow = sr.valid;
             } else {
                 alive = shade_hit(W.R, ps, ray, h, sr) && ps.bounce < W.R.max_depth;
                 want_shadow = sr.valid;
@@ -393,52 +486,54 @@ struct ShadowJob {
 // and a visible light adds d objective / d (light material ka).  Dynamic
 // shared memory: the traversal stacks, then [n_mats][6] gradient floats.
 template <bool F32>
-__global__ void __launch_bounds__(kTraversalBlockMax) wf_shadow_adj(WaveParams W) {
-    extern __shared__ uint2 stack_dyn[];
-    float* grad = reinterpret_cast<float*>(stack_dyn + (size_t)blockDim.x * W.stack_depth);
+__global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) wf_shadow_adj(WaveParams W) {
+    uint2* stacks = stage_top_nodes<F32, true>(W);
+    float* grad = reinterpret_cast<float*>(stacks + (size_t)blockDim.x * W.stack_depth);
     zero_grad_block(grad, W.n_mats);
     Stack st;
-    st.setup(stack_dyn, blockDim.x, W.stack_depth);
+    st.setup(stacks, blockDim.x, W.stack_depth, W.top_nodes);
     ShadowJob<true, F32, true> job(W, st, grad);
-    persistent_loop<false>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], W.queue_chunk, job);
+    persistent_loop<false>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], W.queue_chunk, 31u, job);
     count_rays(W.R.ray_counts, 0, job.rays);
     flush_grad_block(W, grad);
 }
 
-template <bool REFILL, bool WHOLE_LEAF, bool F32>
-__global__ void __launch_bounds__(kTraversalBlockMax) wf_shadow(WaveParams W) {
-    extern __shared__ uint2 stack_dyn[];
+template <bool REFILL, bool WHOLE_LEAF, bool F32, bool TOP>
+__global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) wf_shadow(WaveParams W) {
+    uint2* stacks = stage_top_nodes<F32, TOP>(W);
     Stack st;
-    st.setup(stack_dyn, blockDim.x, W.stack_depth);
+    st.setup(stacks, blockDim.x, W.stack_depth, TOP ? W.top_nodes : 0u);
     ShadowJob<WHOLE_LEAF, F32> job(W, st);
-    persistent_loop<REFILL>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], W.queue_chunk, job);
+    persistent_loop<REFILL>(W.counters[C_SHADOW], &W.counters[C_FETCH_SHD], W.queue_chunk, W.refill_busy, job);
     count_rays(W.R.ray_counts, 0, job.rays);
 }
 
 using WaveKernel = void (*)(WaveParams);
 
-// Kernel variants by the CRT_FLAG_* traversal-scheduling flags and the
-// scene's node format.
-template <bool F32>
+// Kernel variants by the CRT_FLAG_* traversal-scheduling flags, the node
+// format and whether top nodes are staged in shared memory.
+template <bool F32, bool TOP>
 static WaveKernel extend_kernel_f(uint32_t flags) {
     const bool refill = flags & CRT_FLAG_LANE_REFILL, whole = !(flags & CRT_FLAG_SPLIT_LEAF);
-    if (refill) return whole ? wf_extend<true, true, F32> : wf_extend<true, false, F32>;
-    return whole ? wf_extend<false, true, F32> : wf_extend<false, false, F32>;
+    if (refill) return whole ? wf_extend<true, true, F32, TOP> : wf_extend<true, false, F32, TOP>;
+    return whole ? wf_extend<false, true, F32, TOP> : wf_extend<false, false, F32, TOP>;
 }
 
-template <bool F32>
+template <bool F32, bool TOP>
 static WaveKernel shadow_kernel_f(uint32_t flags) {
     const bool refill = flags & CRT_FLAG_LANE_REFILL, whole = !(flags & CRT_FLAG_SPLIT_LEAF);
-    if (refill) return whole ? wf_shadow<true, true, F32> : wf_shadow<true, false, F32>;
-    return whole ? wf_shadow<false, true, F32> : wf_shadow<false, false, F32>;
+    if (refill) return whole ? wf_shadow<true, true, F32, TOP> : wf_shadow<true, false, F32, TOP>;
+    return whole ? wf_shadow<false, true, F32, TOP> : wf_shadow<false, false, F32, TOP>;
 }
 
-static WaveKernel extend_kernel(uint32_t flags, bool f32) {
-    return f32 ? extend_kernel_f<true>(flags) : extend_kernel_f<false>(flags);
+static WaveKernel extend_kernel(uint32_t flags, bool f32, bool top) {
+    if (f32) return top ? extend_kernel_f<true, true>(flags) : extend_kernel_f<true, false>(flags);
+    return top ? extend_kernel_f<false, true>(flags) : extend_kernel_f<false, false>(flags);
 }
 
-static WaveKernel shadow_kernel(uint32_t flags, bool f32) {
-    return f32 ? shadow_kernel_f<true>(flags) : shadow_kernel_f<false>(flags);
+static WaveKernel shadow_kernel(uint32_t flags, bool f32, bool top) {
+    if (f32) return top ? shadow_kernel_f<true, true>(flags) : shadow_kernel_f<true, false>(flags);
+    return top ? shadow_kernel_f<false, true>(flags) : shadow_kernel_f<false, false>(flags);
 }
 
 __global__ void wf_flip(WaveParams W) {
@@ -672,6 +767,8 @@ static WaveParams wave_params(crt_render r, WaveSet& set) {
     W.prof = B.prof.as<unsigned long long>();
     W.stack_depth = (int)traversal_stack(r->opts);
     W.queue_chunk = queue_chunk(r->opts);
+    W.top_nodes = staged_nodes(r->scene, r->opts);
+    W.refill_busy = refill_busy(r->opts);
     return W;
 }
 
@@ -683,14 +780,15 @@ struct WaveGrids {
 };
 
 // Kernel choice and launch shapes, queried before a capture starts.
-static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32, uint32_t block, uint32_t depth) {
+static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32, uint32_t block, uint32_t depth,
+                            uint32_t top_nodes) {
     WaveGrids g;
-    g.extend = extend_kernel(flags, f32);
-    g.shadow = shadow_kernel(flags, f32);
+    g.extend = extend_kernel(flags, f32, top_nodes > 0);
+    g.shadow = shadow_kernel(flags, f32, top_nodes > 0);
     g.extend_count = f32 ? wf_extend_count<true> : wf_extend_count<false>;
     g.shadow_count = f32 ? wf_shadow_count<true> : wf_shadow_count<false>;
     g.tblock = (int)block;
-    g.tsmem = (size_t)block * depth * sizeof(uint2);
+    g.tsmem = (size_t)top_nodes * (f32 ? sizeof(Bvh8FloatNode) : sizeof(Bvh8Node)) + (size_t)block * depth * sizeof(uint2);
     cudaFuncSetAttribute((const void*)g.extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.tsmem);
     cudaFuncSetAttribute((const void*)g.shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.tsmem);
     g.gen = grid_for(capacity, kWaveBlock, 16);
@@ -702,7 +800,8 @@ static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32, uint32_
 }
 
 static WaveGrids wave_grids(crt_render r, uint32_t capacity) {
-    return wave_grids(capacity, r->opts.flags, uses_f32_nodes(r), traversal_block(r->opts), traversal_stack(r->opts));
+    return wave_grids(capacity, r->opts.flags, uses_f32_nodes(r), traversal_block(r->opts), traversal_stack(r->opts),
+                      staged_nodes(r->scene, r->opts));
 }
 
 // Enqueue the body of one wave (generation and every bounce); captured into
@@ -891,13 +990,15 @@ int wavefront_pass(crt_render r, const std::vector<ViewWork>& work) {
 // then the replay re-runs the path and turns each event into gradient terms
 // (WaveGrad) -- so nothing per vertex is stored.
 // ---------------------------------------------------------------------------
-static int ensure_adjoint_buffers(WaveSet& set) {
+static int ensure_adjoint_buffers(WaveSet& set, bool exact) {
     WaveBuffers& B = set.buf;
-    if (B.adj_L.p) return CRT_OK;
     const size_t c = B.capacity;
-    CRT_CUDA(B.adj_L.alloc(c * 16));
-    CRT_CUDA(B.adj_W.alloc(c * 16));
-    CRT_CUDA(B.adj_shadow.alloc(c * 16));
+    if (!B.adj_L.p) {
+        CRT_CUDA(B.adj_L.alloc(c * 16));
+        CRT_CUDA(B.adj_W.alloc(c * 16));
+        CRT_CUDA(B.adj_shadow.alloc(c * 16));
+    }
+    if (exact && !B.adj_hist.p) CRT_CUDA(B.adj_hist.alloc(c * kHistMax * sizeof(uint16_t)));
     return CRT_OK;
 }
 
@@ -920,8 +1021,11 @@ static AdjointGrids adjoint_grids(crt_render r, const WaveGrids& G) {
     return a;
 }
 
-static WaveParams adjoint_params(crt_render r, WaveSet& set, const float4* adj, float* gkd, float* gka) {
+static WaveParams adjoint_params(crt_render r, WaveSet& set, const float4* adj, float* gkd, float* gka,
+                                 uint32_t flags) {
     WaveParams W = wave_params(r, set);
+    W.adj_exact = (flags & CRT_ADJOINT_EXACT_ROULETTE) != 0;
+    W.adj_hist = set.buf.adj_hist.as<uint16_t>();
     W.adj = adj;
     W.st_L = set.buf.adj_L.as<float4>();
     W.st_W = set.buf.adj_W.as<float4>();
@@ -932,15 +1036,19 @@ static WaveParams adjoint_params(crt_render r, WaveSet& set, const float4* adj, 
     return W;
 }
 
-static int capture_adjoint_graph(crt_render r, WaveSet& set, const float4* adj, float* gkd, float* gka) {
-    if (set.adj_graph && set.adj_key[0] == adj && set.adj_key[1] == gkd && set.adj_key[2] == gka) return CRT_OK;
+static int capture_adjoint_graph(crt_render r, WaveSet& set, const float4* adj, float* gkd, float* gka,
+                                 uint32_t flags) {
+    if (set.adj_graph && set.adj_key[0] == adj && set.adj_key[1] == gkd && set.adj_key[2] == gka &&
+        set.adj_flags == flags)
+        return CRT_OK;
     delete static_cast<WaveGraph*>(set.adj_graph);
     WaveGraph* g = new WaveGraph();
     set.adj_graph = g;
     set.adj_key[0] = adj;
     set.adj_key[1] = gkd;
     set.adj_key[2] = gka;
-    const WaveParams W = adjoint_params(r, set, adj, gkd, gka);
+    set.adj_flags = flags;
+    const WaveParams W = adjoint_params(r, set, adj, gkd, gka, flags);
     const WaveGrids G = wave_grids(r, set.buf.capacity);
     const AdjointGrids A = adjoint_grids(r, G);
     CRT_CUDA(cudaGetLastError());
@@ -967,14 +1075,17 @@ static int capture_adjoint_graph(crt_render r, WaveSet& set, const float4* adj, 
 // Waves run on the K sets round-robin, concurrently: gradient sums need no
 // ordering (their atomic adds commute up to rounding).
 int wavefront_adjoint(crt_render r, const std::vector<ViewWork>& work, const float4* adj, float* gkd,
-                      float* gka) {
+                      float* gka, uint32_t flags) {
     if ((size_t)6 * r->scene->n_mats * sizeof(float) > 24u * 1024u)
         return set_error(CRT_ERR_LIMIT, "the adjoint supports at most 1024 materials");
+    const bool exact = (flags & CRT_ADJOINT_EXACT_ROULETTE) != 0;
+    if (exact && r->opts.max_depth > kHistMax)
+        return set_error(CRT_ERR_LIMIT, "CRT_ADJOINT_EXACT_ROULETTE supports max_depth <= 16");
     const uint32_t K = r->opts.wave_sets ? r->opts.wave_sets : kDefaultWaveSets;
     int st = ensure_wave_sets(r, K);
     if (st != CRT_OK) return st;
     for (WaveSet& s : r->sets)
-        if ((st = ensure_adjoint_buffers(s)) != CRT_OK) return st;
+        if ((st = ensure_adjoint_buffers(s, exact)) != CRT_OK) return st;
     const uint32_t cap = r->sets[0].buf.capacity;
     const WavePlan plan = make_waves(r, work, cap);
     if (r->scene_generation != r->scene->generation) {
@@ -990,7 +1101,7 @@ int wavefront_adjoint(crt_render r, const std::vector<ViewWork>& work, const flo
             if ((st = ensure_segments(r->sets[k], segs.size())) != CRT_OK) return st;
         }
     for (WaveSet& s : r->sets)
-        if ((st = capture_adjoint_graph(r, s, adj, gkd, gka)) != CRT_OK) return st;
+        if ((st = capture_adjoint_graph(r, s, adj, gkd, gka, flags)) != CRT_OK) return st;
     CRT_CUDA(cudaEventRecord(r->pass_start, r->stream));
     for (WaveSet& s : r->sets) CRT_CUDA(cudaStreamWaitEvent(s.stream, r->pass_start, 0));
     for (size_t c0 = 0; c0 < plan.waves.size(); c0 += chunk) {
@@ -1219,7 +1330,9 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     W.prof = nullptr;
     W.stack_depth = (int)traversal_stack(o);
     W.queue_chunk = queue_chunk(o);
-    const WaveGrids G = wave_grids(kNoAllocPaths, o.flags, f32, traversal_block(o), W.stack_depth);
+    W.top_nodes = staged_nodes(scene, o);
+    W.refill_busy = refill_busy(o);
+    const WaveGrids G = wave_grids(kNoAllocPaths, o.flags, f32, traversal_block(o), W.stack_depth, W.top_nodes);
     cudaStream_t s = (cudaStream_t)stream;
     DevView view;
     view.cam = R.cam;

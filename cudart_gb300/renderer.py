@@ -59,11 +59,37 @@ def bvh_build_host(positions: np.ndarray, width: int = 8):
 NODE_FORMATS = {"q8": _lib.NODES_Q8, "f32": _lib.NODES_F32}
 
 
+def _face_areas(e1: np.ndarray, e2: np.ndarray) -> np.ndarray:
+    """|e1 x e2| / 2 per face in float32, each operation rounded like the
+    reference's Scene::loadTriangles (length(cross(e1, e2)) / 2)."""
+    cx = e1[:, 1] * e2[:, 2] - e1[:, 2] * e2[:, 1]
+    cy = e1[:, 2] * e2[:, 0] - e1[:, 0] * e2[:, 2]
+    cz = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]
+    return np.sqrt(cx * cx + cy * cy + cz * cz) / np.float32(2.0)
+
+
+def _material_table(materials, kd=None, ka=None):
+    """crt_material array; kd / ka ([n, 3]) override the materials' values."""
+    mats = (Material * len(materials))()
+    for i, m in enumerate(materials):
+        mats[i].bsdf = m.bsdf
+        mats[i].texture = m.tex if m.tex is not None else NO_TEXTURE
+        mats[i].kd[:] = list(map(float, m.kd if kd is None else kd[i]))
+        mats[i].ka[:] = list(map(float, m.ka if ka is None else ka[i]))
+        mats[i].ks[:] = list(map(float, m.ks))
+        mats[i].ns, mats[i].ni, mats[i].diffuse = m.ns, m.ni, m.diffuse
+    return mats
+
+
 class GB300Scene:
     """Scene handle: BVH, triangles, materials, lights and textures on the GPU."""
 
     def __init__(self, sc: SceneArrays, lights: Optional[np.ndarray] = None,
-                 node_format: str = "q8", bvh_width: int = 8):
+                 node_format: str = "q8", bvh_width: int = 8, reference_layout: bool = False):
+        """reference_layout: pass the arrays the way the reference's Scene
+        holds them after construction (CRT_SCENE_EDGES | CRT_SCENE_KA_SCALED:
+        v1/e1/e2 per face, emission already multiplied by 3 x light area),
+        which is what the C++ Renderer shim sends."""
         L = load()
         self.arrays = sc
         self._keep = []
@@ -71,14 +97,22 @@ class GB300Scene:
         nor = np.ascontiguousarray(sc.normals, np.float32)
         uvs = np.ascontiguousarray(sc.uvs, np.float32)
         mid = np.ascontiguousarray(sc.material_ids, np.uint32)
-        mats = (Material * len(sc.materials))()
-        for i, m in enumerate(sc.materials):
-            mats[i].bsdf = m.bsdf
-            mats[i].texture = m.tex if m.tex is not None else NO_TEXTURE
-            mats[i].kd[:] = list(map(float, m.kd))
-            mats[i].ka[:] = list(map(float, m.ka))
-            mats[i].ks[:] = list(map(float, m.ks))
-            mats[i].ns, mats[i].ni, mats[i].diffuse = m.ns, m.ni, m.diffuse
+        flags = 0
+        if reference_layout:
+            p = pos.reshape(-1, 3, 3)
+            e1, e2 = p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]
+            pos = np.ascontiguousarray(np.stack([p[:, 0], e1, e2], axis=1))
+            area = _face_areas(e1, e2)
+            order = lights if lights is not None else sc.light_indices()
+            lights_area = np.float32(0)
+            for f in order:                          # float32, in pick order
+                lights_area = np.float32(lights_area + area[f])
+            ka = np.array([m.ka for m in sc.materials], np.float32)
+            ka = (ka * np.float32(3.0)) * lights_area
+            mats = _material_table(sc.materials, ka=ka)
+            flags = _lib.SCENE_EDGES | _lib.SCENE_KA_SCALED
+        else:
+            mats = _material_table(sc.materials)
         dims = np.asarray([d for img in sc.textures for d in (img.shape[1], img.shape[0])], np.uint32)
         texels = (np.concatenate([texture_texels(img) for img in sc.textures]).astype(np.float32)
                   if sc.textures else np.zeros((1, 3), np.float32))
@@ -90,7 +124,7 @@ class GB300Scene:
                          len(lights) if lights is not None else 0,
                          li.ctypes.data if lights is not None else None,
                          len(sc.textures), dims.ctypes.data if len(dims) else None,
-                         texels.ctypes.data, NODE_FORMATS[node_format], bvh_width)
+                         texels.ctypes.data, NODE_FORMATS[node_format], bvh_width, flags)
         self.node_format = node_format
         self.bvh_width = bvh_width
         h = C.c_void_p()
@@ -108,6 +142,12 @@ class GB300Scene:
         inf = SceneInfo()
         check(load().crt_scene_get_info(self.handle, C.byref(inf)))
         return inf
+
+    def set_materials(self, kd=None, ka=None) -> None:
+        """Replace every material's kd and/or ka ([num_materials, 3] arrays;
+        None keeps the scene's original values)."""
+        mats = _material_table(self.arrays.materials, kd, ka)
+        check(load().crt_scene_set_materials(self.handle, mats, len(mats)))
 
     def set_bvh_width(self, width: int) -> None:
         """Rebuild the BVH with 4 or 8 children per node (same geometry)."""
@@ -149,6 +189,7 @@ class GB300Scene:
 def make_options(max_depth: int = 6, seed: int = 1234, mode: str = "megakernel", view_id: int = 0,
                  wave_paths: int = 0, flags: int = 0, wave_sets: int = 0, block_size: int = 0,
                  stack_depth: int = 0, node_format: Optional[str] = None, queue_chunk: int = 0,
+                 top_nodes: int = 0, refill_busy: int = 0,
                  options: Optional[RenderOptions] = None) -> RenderOptions:
     """crt_render_options from keywords; `options` (e.g. the autotuner's
     choice) overrides them all."""
@@ -167,6 +208,8 @@ def make_options(max_depth: int = 6, seed: int = 1234, mode: str = "megakernel",
     opts.stack_depth = stack_depth
     opts.node_format = -1 if node_format is None else NODE_FORMATS[node_format]
     opts.queue_chunk = queue_chunk
+    opts.top_nodes = top_nodes
+    opts.refill_busy = refill_busy
     return opts
 
 
@@ -178,7 +221,8 @@ class GB300Renderer:
                  mode: str = "megakernel", view_id: int = 0, wave_paths: int = 0,
                  flags: int = 0, wave_sets: int = 0, block_size: int = 0,
                  stack_depth: int = 0, node_format: Optional[str] = None,
-                 queue_chunk: int = 0, options: Optional[RenderOptions] = None):
+                 queue_chunk: int = 0, top_nodes: int = 0, refill_busy: int = 0,
+                 options: Optional[RenderOptions] = None):
         L = load()
         self.scene = scene
         self.width, self.height, self.samples = width, height, samples
@@ -186,7 +230,8 @@ class GB300Renderer:
             camera = camera_from_json(scene.arrays.camera, width, height)
         self.camera = camera
         opts = make_options(max_depth, seed, mode, view_id, wave_paths, flags, wave_sets,
-                            block_size, stack_depth, node_format, queue_chunk, options)
+                            block_size, stack_depth, node_format, queue_chunk, top_nodes, refill_busy,
+                            options)
         self.options = opts
         h = C.c_void_p()
         check(L.crt_render_create(scene.handle, C.byref(camera), width, height, C.byref(opts),
@@ -241,6 +286,21 @@ class GB300Renderer:
     def reset(self) -> None:
         check(load().crt_render_reset(self.handle))
 
+    def load_accum(self, rgb: np.ndarray, samples: int, first_sample: int = 0) -> None:
+        """Resume: install FP32 sums of `samples` samples that started at
+        `first_sample` ([h*w, 3]); the next pass continues after them."""
+        a = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+        check(load().crt_render_load_accum(self.handle, 0, _ptr(a), samples, first_sample))
+
+    def resolve_async(self, pinned_u8) -> None:
+        """Queue resolve + copy into a pinned host buffer (torch uint8 tensor
+        with pin_memory=True, h*w*4 bytes); valid after synchronize()."""
+        check(load().crt_render_resolve_async(self.handle, pinned_u8.data_ptr()))
+
+    def restart(self, first_sample: int) -> None:
+        """Empty accumulator; the next pass starts at sample first_sample."""
+        check(load().crt_render_restart(self.handle, first_sample))
+
     def set_camera(self, camera: Camera) -> None:
         check(load().crt_render_set_camera(self.handle, C.byref(camera)))
         self.camera = camera
@@ -268,12 +328,14 @@ class GB300Renderer:
         return e.value, s.value
 
     def adjoint(self, spp0: int, n_spp: int, adjoint_ptr: int, grad_kd_ptr: int, grad_ka_ptr: int,
-                stream: Optional[int] = None) -> None:
+                exact_roulette: bool = False) -> None:
         """Path-replay adjoint over device buffers (see crt_render_adjoint):
         adds d<adjoint, radiance sum of samples [spp0, spp0+n_spp)>/d(kd, ka)
         to the [num_materials][3] float buffers.  Runs on the handle's stream
         (synchronize() before reading the gradients)."""
-        check(load().crt_render_adjoint(self.handle, spp0, n_spp, adjoint_ptr, grad_kd_ptr, grad_ka_ptr))
+        flags = _lib.ADJOINT_EXACT_ROULETTE if exact_roulette else 0
+        check(load().crt_render_adjoint(self.handle, spp0, n_spp, adjoint_ptr, grad_kd_ptr, grad_ka_ptr,
+                                        flags))
 
 
 class GB300Batch:

@@ -110,7 +110,17 @@ typedef struct {
     uint32_t node_format;          /* crt_node_format renders use by default; both
                                       encodings are uploaded */
     uint32_t bvh_width;            /* children per node: 4 or 8 (0 = 8) */
+    uint32_t flags;                /* crt_scene_flags */
 } crt_scene_desc;
+
+/* Inputs as the reference's Scene holds them after construction, so a
+ * Renderer shim can pass its arrays unchanged: */
+typedef enum {
+    CRT_SCENE_EDGES = 1u,      /* positions are v1, e1, e2 per face (Triangle::_v1,
+                                  _e1, _e2) instead of three vertices */
+    CRT_SCENE_KA_SCALED = 2u   /* material ka already includes the emission
+                                  scaling Ka * 3 * lights area (scene.cpp:163,177) */
+} crt_scene_flags;
 
 /* BVH node encoding on the device (same tree either way). */
 typedef enum {
@@ -164,6 +174,12 @@ CRT_EXPORT int crt_scene_get_info(crt_scene scene, crt_scene_info* out);
  * triangle records [num_triangles][48 bytes] (v1.xyz + face index bits,
  * e1.xyz + 0, e2.xyz + 0).  Either pointer may be NULL. */
 CRT_EXPORT int crt_scene_export_bvh(crt_scene scene, void* nodes, void* triangles);
+/* Replaces the material table (n = the scene's material count; ka is taken
+ * as crt_scene_create took it, scaled or not per CRT_SCENE_KA_SCALED).  The light list and the total light
+ * area stay those of crt_scene_create.  Waits for the device to go idle
+ * first, so passes already queued finish with the old table.
+ * No reference counterpart (the optimisation loop of the adjoint). */
+CRT_EXPORT int crt_scene_set_materials(crt_scene scene, const crt_material* materials, uint32_t n);
 /* Rebuilds the scene's BVH with 4 or 8 children per node from its own
  * triangle records (the geometry is unchanged, so every query answers the
  * same) and uploads it in place of the current one; the autotuner's BVH
@@ -230,6 +246,14 @@ typedef struct {
     uint32_t queue_chunk;      /* wavefront traversal kernels: queue entries a warp
                                   claims per fetch, 32, 64, 128 or 256 (0 = 32);
                                   unused with CRT_FLAG_LANE_REFILL */
+    uint32_t top_nodes;        /* wavefront traversal kernels: the first top_nodes
+                                  BVH nodes (breadth-first: the top levels) are
+                                  copied to shared memory at kernel start, 0..128
+                                  (0 = none; 9 = two levels, 73 = three) */
+    uint32_t refill_busy;      /* with CRT_FLAG_LANE_REFILL: idle lanes of a warp
+                                  take new rays together once at most this many
+                                  lanes are still busy, 1..31 (0 = 31: as soon as
+                                  one lane is idle) */
 } crt_render_options;
 
 CRT_EXPORT void crt_render_options_default(crt_render_options* opts);
@@ -248,11 +272,35 @@ CRT_EXPORT int crt_render_synchronize(crt_render r);
  * float3ToUchar4 (renderer.h:149-156) then gammaCorrectPixel
  * (renderer.cu:495-504); host_rgba holds width*height*4 bytes. */
 CRT_EXPORT int crt_render_resolve(crt_render r, uint8_t* host_rgba);
+/* renderKernel's own device image (parallel_renderer.cu:338-341): RGBA8 of
+ * the average through float3ToUchar4 only (the gamma table is applied on
+ * the host by copyImageBytes), written to the caller's device buffer of
+ * width*height*4 bytes on the handle's stream.  Asynchronous. */
+CRT_EXPORT int crt_render_resolve_device(crt_render r, void* d_rgba);
+/* crt_render_resolve without the wait: the resolve kernel and the copy into
+ * host_rgba (pinned memory, width*height*4 bytes) are queued on the handle's
+ * stream behind the passes already queued, so a caller can queue the next
+ * pass right away and overlap it with the copy; the bytes are valid after
+ * crt_render_synchronize.  Uses a device staging buffer owned by the handle.
+ * No reference counterpart. */
+CRT_EXPORT int crt_render_resolve_async(crt_render r, uint8_t* host_rgba);
+/* Progressive resume: replaces the accumulator of view `view` with
+ * host_rgb ([width*height][3] FP32 sums, as crt_render_view_accum returns
+ * them) holding `samples` samples that started at sample index
+ * `first_sample`; the next pass continues at first_sample + samples.  With
+ * the sums and the two counters saved, a render resumes bit for bit where it
+ * stopped.  No reference counterpart. */
+CRT_EXPORT int crt_render_load_accum(crt_render r, uint32_t view, const float* host_rgb, uint32_t samples,
+                                     uint32_t first_sample);
 /* FP32 per-pixel radiance sums [width*height][3] (host copy). */
 CRT_EXPORT int crt_render_accum(crt_render r, float* host_rgb);
 /* Device pointer of the accumulator, valid until destroy. */
 CRT_EXPORT int crt_render_accum_device(crt_render r, float** d_rgb);
 CRT_EXPORT int crt_render_reset(crt_render r);
+/* As crt_render_reset, but the next pass renders from sample index
+ * first_sample on (every view): a fresh, independent estimate per call, as
+ * an optimisation loop wants.  No reference counterpart. */
+CRT_EXPORT int crt_render_restart(crt_render r, uint32_t first_sample);
 CRT_EXPORT int crt_render_set_camera(crt_render r, const crt_camera* camera);
 /* Use the caller's CUDA stream (cudaStream_t) instead of the handle's own. */
 CRT_EXPORT int crt_render_set_stream(crt_render r, void* stream);
@@ -319,15 +367,22 @@ CRT_EXPORT int crt_render_view_accum(crt_render r, uint32_t view, float* host_rg
  * I = accum / spp, pass adjoint = dL/dI / spp.
  * Path-replay backpropagation: each path is traced twice from the same
  * Philox counters, first for its radiance, then again turning every vertex
- * into gradient terms, so nothing per vertex is stored; Russian roulette's
- * survival probability counts as a constant.  Gradients are summed per warp
- * and block before global atomics.  Always the wavefront form.
+ * into gradient terms, so nothing per vertex is stored.  By default Russian
+ * roulette's survival probability counts as a constant: the gradient is
+ * unbiased for the expected image (roulette is unbiased whatever the
+ * probability).  CRT_ADJOINT_EXACT_ROULETTE also differentiates the
+ * division by max(throughput) after each surviving roulette: the exact
+ * derivative of every sample with its decisions held, what central finite
+ * differences with common random numbers measure (max_depth <= 16; keeps a
+ * 16-entry material history per path).  Gradients are summed per warp and
+ * block before global atomics.  Always the wavefront form.
  * d_adjoint: device float4 per pixel of every view (the layout of
  * crt_render_accum_device; .w ignored).  d_grad_kd, d_grad_ka: device float
  * [num_materials][3], ADDED to.  At most 1024 materials.  Asynchronous on the
  * handle's stream; the accumulator and sample counts do not change. */
+enum { CRT_ADJOINT_EXACT_ROULETTE = 1u };
 CRT_EXPORT int crt_render_adjoint(crt_render r, uint32_t spp0, uint32_t n_spp, const float* d_adjoint,
-                                  float* d_grad_kd, float* d_grad_ka);
+                                  float* d_grad_kd, float* d_grad_ka, uint32_t flags);
 
 /* ---- allocation-free tile render ----------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
@@ -368,7 +423,8 @@ CRT_EXPORT int crt_render_ray_counts(crt_render r, uint64_t* extension_rays, uin
  * short wavefront renders of the given scene, camera and image size and
  * searches, by coordinate descent, the options that change speed but not
  * the image: node_format, block_size, stack_depth, queue_chunk, wave_sets,
- * wave_paths, CRT_FLAG_LANE_REFILL and (tune_bvh_width) the BVH width.
+ * wave_paths, CRT_FLAG_LANE_REFILL, top_nodes and (tune_bvh_width) the BVH
+ * width.
  * The device must be otherwise idle for the timings to mean anything.  With
  * tune_bvh_width the scene's BVH is rebuilt (crt_scene_set_bvh_width) and
  * the faster width is left in place. */

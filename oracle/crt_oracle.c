@@ -495,8 +495,39 @@ static inline void reset_ray(orc_ray* r, orc_f3 o, orc_f3 d) {
     r->o = o; r->d = d; r->tmin = ORC_EPS; r->tmax = FLT_MAX; r->idx = -1; r->u = r->v = 0.f;
 }
 
+/* Gradient context of the adjoint replay (orc_adjoint): w is the pixel's
+ * adjoint weight, total the radiance of the path's first trace; the
+ * gradient terms are formed and summed in FP64. */
+typedef struct {
+    double w[3];
+    orc_f3 total;
+    double ka_scale;            /* d(stored emission)/d(material ka) = 3 * lights area */
+    double* gkd;                /* [n_mats][3] */
+    double* gka;
+    /* exact roulette: materials of the kd factors in the throughput so far,
+     * and the previous surviving roulette's channel and history length */
+    int exact;
+    uint32_t hist[64];
+    int n_hist, prev_c, prev_n;
+} orc_grad;
+
+static orc_f3 sample_path(const orc_scene* s, const orc_camera* cam, int x, int y,
+                          orc_sampler* smp, uint32_t max_depth, orc_grad* g);
+
 orc_f3 orc_sample_pixel(const orc_scene* s, const orc_camera* cam, int x, int y,
                         orc_sampler* smp, uint32_t max_depth) {
+    return sample_path(s, cam, x, y, smp, max_depth, NULL);
+}
+
+/* samplePixel with optional gradient hooks: with g, each event of the path
+ * adds its derivative terms (path-replay backpropagation; Russian roulette's
+ * survival probability held constant):
+ *  - emission term mask * ka / lights_area:  d/d ka_m = mask * 3 SA / SA;
+ *  - diffuse vertex of untextured material m: every later term carries one
+ *    factor kd_m, so d/d kd_m += (total - radiance so far) / kd_m;
+ *  - visible light sample: d/d ka_light = mask * weight * 3 SA. */
+static orc_f3 sample_path(const orc_scene* s, const orc_camera* cam, int x, int y,
+                          orc_sampler* smp, uint32_t max_depth, orc_grad* g) {
     orc_ray ray;
     camera_ray(cam, x, y, smp, &ray);
     orc_f3 color = f3(0.f, 0.f, 0.f);
@@ -512,8 +543,14 @@ orc_f3 orc_sample_pixel(const orc_scene* s, const orc_camera* cam, int x, int y,
         uint32_t hit = (uint32_t)ray.idx;
         const orc_triangle* tri = &s->tris[hit];
         const orc_material* m = &s->mats[tri->material];
-        if (bounce == 0 || prev == ORC_SPECULAR || prev == ORC_REFRACTIVE)
+        if (bounce == 0 || prev == ORC_SPECULAR || prev == ORC_REFRACTIVE) {
             color = add3(color, muls(mul3(mask, m->ka), one_over_sa));
+            if (g) {
+                const double mk[3] = {mask.x, mask.y, mask.z};
+                for (int c = 0; c < 3; ++c)
+                    g->gka[3 * tri->material + c] += g->w[c] * mk[c] * g->ka_scale * (double)one_over_sa;
+            }
+        }
         orc_f3 normal = tri_normal(tri, ray.u, ray.v);
         orc_f3 position = add3(add3(ray.o, muls(ray.d, ray.tmax)), muls(normal, ORC_EPS2));
         orc_f3 out_dir = normalize3(ray.d);
@@ -572,6 +609,13 @@ orc_f3 orc_sample_pixel(const orc_scene* s, const orc_camera* cam, int x, int y,
                 float uvx = tri->uv1.x * tw + tri->uv2.x * tu + tri->uv3.x * tv;
                 float uvy = tri->uv1.y * tw + tri->uv2.y * tu + tri->uv3.y * tv;
                 kd = sample_texture(s, m->tex, uvx, uvy);
+            } else if (g) {
+                const double rest[3] = {(double)g->total.x - color.x, (double)g->total.y - color.y,
+                                        (double)g->total.z - color.z};
+                const double k[3] = {kd.x, kd.y, kd.z};
+                for (int c = 0; c < 3; ++c)
+                    if (k[c] != 0.0) g->gkd[3 * tri->material + c] += g->w[c] * rest[c] / k[c];
+                if (g->exact && g->n_hist < 64) g->hist[g->n_hist++] = tri->material;
             }
             mask = divs(mul3(mask, muls(kd, cosw)), 0.5f);
             /* light pick, renderer.cu:218-221 */
@@ -595,6 +639,11 @@ orc_f3 orc_sample_pixel(const orc_scene* s, const orc_camera* cam, int x, int y,
                     float cost = fabsf(dot3(tri_normal(lt, sr.u, sr.v), muls(sr.d, -1.0f)));
                     float wgt = sa / (d2 * s->lights_area) * cost;
                     direct = add3(direct, muls(lcolor, wgt));
+                    if (g) {
+                        const double mk[3] = {mask.x, mask.y, mask.z};
+                        for (int c = 0; c < 3; ++c)
+                            g->gka[3 * lt->material + c] += g->w[c] * mk[c] * (double)wgt * g->ka_scale;
+                    }
                 }
             }
             color = add3(color, mul3(mask, direct));
@@ -608,6 +657,30 @@ orc_f3 orc_sample_pixel(const orc_scene* s, const orc_camera* cam, int x, int y,
         if (bounce >= 3) {                                   /* renderer.cu:252-259 */
             float p = maxc3(mask);
             if (orc_next_float(smp) > p) break;
+            if (g && g->exact) {
+                /* After this roulette the throughput is mask / mask[c], c the
+                 * channel max_component picks: every term from here on gets
+                 * -1/kd[c] per kd factor so far, in channel c, replacing the
+                 * previous roulette's correction (only the latest counts). */
+                const int c01 = mask.x > mask.y ? 0 : 1;
+                const float v01 = mask.x > mask.y ? mask.x : mask.y;
+                const int cs = v01 > mask.z ? c01 : 2;
+                const double sdot = g->w[0] * ((double)g->total.x - color.x) +
+                                    g->w[1] * ((double)g->total.y - color.y) +
+                                    g->w[2] * ((double)g->total.z - color.z);
+                for (int i = 0; i < g->n_hist; ++i) {
+                    const orc_f3 k = s->mats[g->hist[i]].kd;
+                    const double kc = cs == 0 ? k.x : cs == 1 ? k.y : k.z;
+                    if (kc != 0.0) g->gkd[3 * g->hist[i] + cs] -= sdot / kc;
+                }
+                for (int i = 0; i < g->prev_n; ++i) {
+                    const orc_f3 k = s->mats[g->hist[i]].kd;
+                    const double kc = g->prev_c == 0 ? k.x : g->prev_c == 1 ? k.y : k.z;
+                    if (kc != 0.0) g->gkd[3 * g->hist[i] + g->prev_c] += sdot / kc;
+                }
+                g->prev_c = cs;
+                g->prev_n = g->n_hist;
+            }
             mask = divs(mask, p);
         }
     }
@@ -644,6 +717,57 @@ void orc_render(const orc_scene* s, const orc_camera* cam, uint64_t seed, uint32
         if (acc) { acc[3 * k] = a[0]; acc[3 * k + 1] = a[1]; acc[3 * k + 2] = a[2]; }
         if (mean) for (int ch = 0; ch < 3; ++ch) mean[3 * k + ch] = mu[ch];
         if (m2) for (int ch = 0; ch < 3; ++ch) m2[3 * k + ch] = q[ch];
+    }
+    (void)H;
+    (void)threads;
+}
+
+void orc_adjoint(const orc_scene* s, const orc_camera* cam, uint64_t seed, uint32_t view,
+                 uint32_t spp0, uint32_t spp, uint32_t max_depth, const float* adjoint,
+                 uint32_t n_mats, double* grad_kd, double* grad_ka, int exact_roulette, int threads) {
+    uint32_t W = (uint32_t)cam->xpixels, H = (uint32_t)cam->ypixels;
+    int64_t total = (int64_t)W * H;
+    const double ka_scale = 3.0 * (double)s->lights_area;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel
+#endif
+    {
+        double* gkd = (double*)calloc(3 * (size_t)n_mats, sizeof(double));
+        double* gka = (double*)calloc(3 * (size_t)n_mats, sizeof(double));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+        for (int64_t k = 0; k < total; ++k) {
+            const float* a = adjoint + 3 * k;
+            if (a[0] == 0.f && a[1] == 0.f && a[2] == 0.f) continue;
+            int x = (int)((uint32_t)k % W), y = (int)((uint32_t)k / W);
+            for (uint32_t si = 0; si < spp; ++si) {
+                orc_sampler smp;
+                orc_sampler_init(&smp, seed, view, (uint32_t)k, spp0 + si);
+                orc_grad g;
+                g.w[0] = a[0]; g.w[1] = a[1]; g.w[2] = a[2];
+                g.ka_scale = ka_scale;
+                g.gkd = gkd;
+                g.gka = gka;
+                g.exact = exact_roulette;
+                g.n_hist = 0;
+                g.prev_c = 0;
+                g.prev_n = 0;
+                g.total = sample_path(s, cam, x, y, &smp, max_depth, NULL);
+                orc_sampler_init(&smp, seed, view, (uint32_t)k, spp0 + si);   /* replay */
+                sample_path(s, cam, x, y, &smp, max_depth, &g);
+            }
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        for (uint32_t i = 0; i < 3 * n_mats; ++i) {
+            grad_kd[i] += gkd[i];
+            grad_ka[i] += gka[i];
+        }
+        free(gkd);
+        free(gka);
     }
     (void)H;
     (void)threads;

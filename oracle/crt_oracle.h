@@ -166,6 +166,21 @@ void orc_render(const orc_scene* s, const orc_camera* cam, uint64_t seed, uint32
                 const uint32_t* pixels, uint32_t n_pixels,
                 float* acc, double* mean, double* m2, int threads);
 
+/* FP64 reference gradient of  sum_p,c adjoint[p][c] * S[p][c]  (S = the
+ * radiance sum of samples [spp0, spp0+spp) of pixel p) with respect to each
+ * material's kd (untextured diffuse vertices) and ka (emission as given,
+ * stored as ka * 3 * lights_area): each path is traced, then replayed from
+ * the same sampler with every event turned into derivative terms, summed in
+ * FP64.  exact_roulette = 0: Russian roulette's survival probability is held
+ * constant (unbiased for the gradient of the expected image); 1: its
+ * renormalisation mask / max(mask) is differentiated too, the exact
+ * derivative of each sample with its decisions fixed (what central
+ * differences with common random numbers measure; kd history of at most 64
+ * vertices).  adjoint [W*H][3]; grad_kd / grad_ka [n_mats][3] are added to. */
+void orc_adjoint(const orc_scene* s, const orc_camera* cam, uint64_t seed, uint32_t view,
+                 uint32_t spp0, uint32_t spp, uint32_t max_depth, const float* adjoint,
+                 uint32_t n_mats, double* grad_kd, double* grad_ka, int exact_roulette, int threads);
+
 /* ---- output formatting -------------------------------------------------- */
 /* float3ToUchar4 (renderer.h:149-156) of acc / spp, then gammaCorrectPixel
  * (renderer.cu:495-504) on the host (parallel_renderer.cu:303-310). */

@@ -71,6 +71,8 @@ def lib():
         L.orc_traversal_counts.argtypes = [P, P, C.c_uint32, P, P]
         L.orc_render.argtypes = [P, P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, P, C.c_uint32, P, P, P, C.c_int]
+        L.orc_adjoint.argtypes = [P, P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                  P, C.c_uint32, P, P, C.c_int, C.c_int]
         L.orc_resolve.argtypes = [P, C.c_uint32, C.c_uint32, P]
         L.orc_gamma_u8.argtypes = [C.c_uint8]
         L.orc_gamma_u8.restype = C.c_uint8
@@ -198,6 +200,20 @@ class OracleScene:
                          _p(px) if px is not None else None, npx, _p(acc), _p(mean), _p(m2),
                          threads)
         return acc, mean, m2
+
+    def adjoint(self, camera: np.ndarray, seed: int, spp: int, max_depth: int, adjoint: np.ndarray,
+                *, view: int = 0, spp0: int = 0, exact_roulette: bool = False, threads: int = 0):
+        """FP64 reference gradient of sum(adjoint * radiance sum of samples
+        [spp0, spp0+spp)) w.r.t. each material's kd and ka: (grad_kd,
+        grad_ka), float64 [n_mats, 3].  adjoint: [W*H, 3]."""
+        W, H = int(camera["xpixels"][0]), int(camera["ypixels"][0])
+        adj = np.ascontiguousarray(adjoint, np.float32).reshape(W * H, 3)
+        n = len(self.mats)
+        gkd = np.zeros((n, 3), np.float64)
+        gka = np.zeros((n, 3), np.float64)
+        lib().orc_adjoint(self.ptr, _p(camera), seed, view, spp0, spp, max_depth, _p(adj), n,
+                          _p(gkd), _p(gka), int(exact_roulette), threads)
+        return gkd, gka
 
 
 def resolve(acc: np.ndarray, spp: int) -> np.ndarray:

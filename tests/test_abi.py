@@ -103,3 +103,18 @@ def test_camera_from_json_matches_oracle():
         c = camera_from_json(spec, w, h)
         o = oracle.make_camera(spec, w, h)
         assert bytes(c) == o.tobytes()
+
+
+def test_renderer_shim_compiles_against_the_reference_headers():
+    """The C++ Renderer subclass for the reference's tree compiles against the
+    reference's own headers (where its sources are present)."""
+    import shutil
+    import subprocess
+    shim = os.path.join(ROOT, "cudart_gb300", "shim")
+    if shutil.which("nvcc") is None or shutil.which("make") is None:
+        pytest.skip("nvcc/make not available")
+    ref = subprocess.run(["make", "-s", "-C", shim, "print-ref"], capture_output=True, text=True).stdout.strip()
+    if not os.path.isdir(os.path.join(ref, "src", "include")):
+        pytest.skip("reference sources not present")
+    res = subprocess.run(["make", "-C", shim, "check"], capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout + res.stderr

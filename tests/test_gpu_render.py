@@ -66,7 +66,9 @@ def test_f32_nodes_render_identically(cuda, mode):
 
 @pytest.mark.parametrize("shape", [dict(block_size=64), dict(block_size=256),
                                    dict(stack_depth=4), dict(stack_depth=32, block_size=256),
-                                   dict(node_format="f32"), dict(wave_sets=1), dict(wave_sets=8)])
+                                   dict(node_format="f32"), dict(wave_sets=1), dict(wave_sets=8),
+                                   dict(top_nodes=9), dict(top_nodes=73, node_format="f32"),
+                                   dict(top_nodes=128, block_size=64, queue_chunk=128)])
 def test_launch_shape_does_not_change_results(cuda, shape):
     """Block size, shared stack depth, per-render node format and the
     number of wave sets are scheduling choices: the image is unchanged."""
@@ -89,6 +91,54 @@ def test_four_wide_bvh_renders_identically(cuda):
     a.render()
     b.render()
     assert np.array_equal(a.accum(), b.accum())
+
+
+def test_reference_layout_renders_identically(cuda):
+    """The arrays the C++ Renderer shim passes (v1/e1/e2 per face, emission
+    already scaled by 3 x light area) give the scene the standard arrays give."""
+    sc = scenes.feature_mix(width=64, height=48)
+    a = GB300Scene(sc)
+    b = GB300Scene(sc, reference_layout=True)
+    assert a.info.lights_area == b.info.lights_area
+    out = []
+    for g in (a, b):
+        r = GB300Renderer(g, sc.width, sc.height, 8, max_depth=6, mode="wavefront")
+        r.render()
+        out.append(r.accum())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_resume_from_saved_accumulator(cuda):
+    """Save the sums and counters after some passes, load them into a fresh
+    handle, continue: the result equals the uninterrupted render."""
+    sc = scenes.cornell_box(width=64, height=48)
+    g = GB300Scene(sc)
+    full = GB300Renderer(g, 64, 48, 10, max_depth=5, mode="wavefront")
+    full.render(10)
+    part = GB300Renderer(g, 64, 48, 10, max_depth=5, mode="wavefront")
+    part.render(4)
+    saved, n = part.accum(), part.get_samples_rendered()
+    resumed = GB300Renderer(g, 64, 48, 10, max_depth=5, mode="megakernel")
+    resumed.load_accum(saved, n, 0)
+    resumed.render(6)
+    assert resumed.get_samples_rendered() == 10
+    assert np.array_equal(resumed.accum(), full.accum())
+    assert np.array_equal(resumed.copy_image_bytes(), full.copy_image_bytes())
+
+
+def test_resolve_async_overlaps_next_pass(cuda):
+    torch = cuda
+    sc = scenes.cornell_box(width=64, height=48)
+    g = GB300Scene(sc)
+    r = GB300Renderer(g, 64, 48, 8, max_depth=5, mode="wavefront")
+    r.render(4)
+    buf = torch.empty(64 * 48 * 4, dtype=torch.uint8).pin_memory()
+    r.resolve_async(buf)
+    r.render(4)              # queued behind the copy
+    r.synchronize()
+    ref = GB300Renderer(g, 64, 48, 4, max_depth=5, mode="wavefront")
+    ref.render(4)
+    assert np.array_equal(buf.numpy().reshape(48, 64, 4), ref.copy_image_bytes())
 
 
 def test_progressive_passes_equal_single(cuda):

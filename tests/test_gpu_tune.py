@@ -45,7 +45,7 @@ def test_rebuilt_bvh_keeps_results_and_renders_follow(cuda):
 
 
 @pytest.mark.parametrize("bad", [dict(block_size=96), dict(stack_depth=2), dict(stack_depth=40),
-                                 dict(queue_chunk=48), dict(wave_sets=9)])
+                                 dict(queue_chunk=48), dict(wave_sets=9), dict(top_nodes=129)])
 def test_bad_launch_options_are_rejected(cuda, bad):
     sc = scenes.cornell_box(width=32, height=32)
     g = GB300Scene(sc)
