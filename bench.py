@@ -328,9 +328,11 @@ def run_gb300(args):
         opts.seed, opts.view_id = 1234, rank
         wf = GB300Renderer(scene, sc.width, sc.height, spp, options=opts)
     else:
-        # each rank renders its own Philox streams of the same frame (view_id = rank)
+        # each rank renders its own Philox streams of the same frame (view_id = rank);
+        # --options sets launch options by hand (e.g. to profile one variant)
+        extra = json.loads(args.options) if args.options else {}
         wf = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
-                           mode="wavefront", view_id=rank)
+                           mode="wavefront", view_id=rank, **extra)
     wf.set_stream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -498,6 +500,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="480x270 reduced scene (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="default launch options, no autotuner")
+    ap.add_argument("--options", default="", help='with --no-tune: launch options as JSON, e.g. {"node_format": "f32"}')
     ap.add_argument("--no-extra", action="store_true", help="skip the batched-views and adjoint legs")
     ap.add_argument("--c4-spp-div", type=int, default=4, help="batched views: spp divisor")
     ap.add_argument("--inversion-iters", type=int, default=200)

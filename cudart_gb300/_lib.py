@@ -103,6 +103,7 @@ SCENE_EDGES = 1
 SCENE_KA_SCALED = 2
 FLAG_LANE_REFILL = 1
 FLAG_SPLIT_LEAF = 2
+FLAG_OCTANT_QUEUES = 4
 
 
 # name -> (restype, argtypes); every entry point of include/crt_gb300.h

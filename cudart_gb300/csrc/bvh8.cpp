@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <future>
+#include <mutex>
 #include <thread>
 
 namespace crt {
@@ -149,17 +150,40 @@ struct Builder {
     }
 
     // Builds idx[start, end) into `out`; returns the subtree root index.
-    int32_t build(uint32_t start, uint32_t end, std::vector<Node2>& out, int par_depth) const {
-        Box nb, cb;
-        nb.reset();
-        cb.reset();
-        for (uint32_t i = start; i < end; ++i) {
+    // Bounds of the triangles and of the centroids of idx[s, e).
+    void bounds(uint32_t s, uint32_t e, Box& nb, Box& cb) const {
+        for (uint32_t i = s; i < e; ++i) {
             uint32_t t = idx[i];
             nb.grow(tbox[t]);
             for (int k = 0; k < 3; ++k) {
                 cb.lo[k] = std::min(cb.lo[k], cent[3 * t + k]);
                 cb.hi[k] = std::max(cb.hi[k], cent[3 * t + k]);
             }
+        }
+    }
+
+    int32_t build(uint32_t start, uint32_t end, std::vector<Node2>& out, int par_depth) const {
+        Box nb, cb;
+        nb.reset();
+        cb.reset();
+        const uint32_t parts = end - start >= (1u << 16) ? std::min<unsigned>(hw_threads, (end - start) >> 15) : 1u;
+        if (parts > 1) {   // min / max merge exactly, in any order
+            std::vector<Box> pn(parts), pc(parts);
+            std::vector<std::thread> pool;
+            for (uint32_t p = 0; p < parts; ++p) {
+                pn[p].reset();
+                pc[p].reset();
+                const uint32_t s = start + (uint32_t)((uint64_t)(end - start) * p / parts);
+                const uint32_t e = start + (uint32_t)((uint64_t)(end - start) * (p + 1) / parts);
+                pool.emplace_back([&, p, s, e] { bounds(s, e, pn[p], pc[p]); });
+            }
+            for (std::thread& t : pool) t.join();
+            for (uint32_t p = 0; p < parts; ++p) {
+                nb.grow(pn[p]);
+                cb.grow(pc[p]);
+            }
+        } else {
+            bounds(start, end, nb, cb);
         }
         int32_t me = (int32_t)out.size();
         out.emplace_back();
@@ -232,28 +256,36 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
     if (max_children != 4 && max_children != 8) { *msg = "BVH width must be 4 or 8"; return false; }
     if (n == 0) { *msg = "scene has no triangles"; return false; }
     // Margin: 2^-15 of the largest coordinate magnitude (at least 2^-15).
+    std::mutex scale_mutex;
     double scale = 1.0;
-    for (uint64_t i = 0; i < 3ull * n; ++i) {
-        scale = std::max(scale, (double)std::fabs(v1[i]));
-        scale = std::max(scale, (double)std::fabs(v1[i] + e1[i]));
-        scale = std::max(scale, (double)std::fabs(v1[i] + e2[i]));
-    }
+    parallel_for(n, [&](size_t t0, size_t t1) {
+        double s = 1.0;
+        for (uint64_t i = 3 * t0; i < 3 * t1; ++i) {
+            s = std::max(s, (double)std::fabs(v1[i]));
+            s = std::max(s, (double)std::fabs(v1[i] + e1[i]));
+            s = std::max(s, (double)std::fabs(v1[i] + e2[i]));
+        }
+        std::lock_guard<std::mutex> lock(scale_mutex);
+        scale = std::max(scale, s);
+    });
     const float margin = (float)std::ldexp(scale, -15);
     std::vector<Box> tbox(n);
     std::vector<float> cent(3ull * n);
-    for (uint32_t t = 0; t < n; ++t) {
-        for (int k = 0; k < 3; ++k) {
-            double a = v1[3 * t + k];
-            double b = a + (double)e1[3 * t + k];
-            double c = a + (double)e2[3 * t + k];
-            double lo = std::min(a, std::min(b, c)), hi = std::max(a, std::max(b, c));
-            tbox[t].lo[k] = (float)(lo - margin);
-            tbox[t].hi[k] = (float)(hi + margin);
-            if ((double)tbox[t].lo[k] > lo - margin) tbox[t].lo[k] = std::nextafter(tbox[t].lo[k], -FLT_MAX);
-            if ((double)tbox[t].hi[k] < hi + margin) tbox[t].hi[k] = std::nextafter(tbox[t].hi[k], FLT_MAX);
-            cent[3 * t + k] = 0.5f * (tbox[t].lo[k] + tbox[t].hi[k]);
+    parallel_for(n, [&](size_t t0, size_t t1) {
+        for (size_t t = t0; t < t1; ++t) {
+            for (int k = 0; k < 3; ++k) {
+                double a = v1[3 * t + k];
+                double b = a + (double)e1[3 * t + k];
+                double c = a + (double)e2[3 * t + k];
+                double lo = std::min(a, std::min(b, c)), hi = std::max(a, std::max(b, c));
+                tbox[t].lo[k] = (float)(lo - margin);
+                tbox[t].hi[k] = (float)(hi + margin);
+                if ((double)tbox[t].lo[k] > lo - margin) tbox[t].lo[k] = std::nextafter(tbox[t].lo[k], -FLT_MAX);
+                if ((double)tbox[t].hi[k] < hi + margin) tbox[t].hi[k] = std::nextafter(tbox[t].hi[k], FLT_MAX);
+                cent[3 * t + k] = 0.5f * (tbox[t].lo[k] + tbox[t].hi[k]);
+            }
         }
-    }
+    });
     std::vector<uint32_t> idx(n);
     for (uint32_t i = 0; i < n; ++i) idx[i] = i;
     Builder b{tbox.data(), cent.data(), idx.data(), std::max(1u, std::thread::hardware_concurrency())};

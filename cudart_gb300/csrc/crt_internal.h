@@ -68,6 +68,7 @@ struct crt_scene_s {
 struct WaveBuffers {
     uint32_t capacity = 0;
     uint32_t seg_capacity = 0;      // wave segments the segs buffer holds
+    bool octant = false;            // queues hold 8 octant regions
     crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, counters, waves, segs, prof;
     crt::DevBuf adj_L, adj_W, adj_shadow, adj_hist;   // adjoint replay state, allocated on first use
 };

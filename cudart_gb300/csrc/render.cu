@@ -24,7 +24,12 @@ constexpr uint32_t kMegaSppPerLaunch = 4;
 // accumulator in sample order, so the sums equal the reference's per-pass
 // accumulation (`p_imgBuffer[idx] += color`, parallel_renderer.cu:340).
 template <bool F32>
-__global__ void __launch_bounds__(kMegaBlock) mega_kernel(RenderParams P) {
+// Register cap of the megakernel (the whole path lives in registers):
+// measured 80 best against 64, 96 and the uncapped 128.
+#ifndef CRT_MEGA_REGS
+#define CRT_MEGA_REGS 80
+#endif
+__global__ void __maxnreg__(F32 ? CRT_MEGA_REGS + 16 : CRT_MEGA_REGS) mega_kernel(RenderParams P) {
     __shared__ uint2 stack_sh[kStackShared * kMegaBlock];
     Stack st;
     st.setup(stack_sh, kMegaBlock, kStackShared);

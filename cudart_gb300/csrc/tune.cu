@@ -41,12 +41,13 @@ struct Tuner {
     std::map<Key, float> seen;   // measured ms per sample per pixel
     uint32_t candidates = 0;
 
-    // Path-state bytes of a candidate: 172 bytes per path per wave set
-    // (five float4 records, two queue words, one shadow request).
+    // Path-state bytes of a candidate: 136 bytes per path per wave set
+    // (five float4 records, two queue words, one shadow request), plus 56
+    // more with octant-binned queues.
     uint64_t wave_bytes(const crt_render_options& o) const {
         const uint64_t paths = o.wave_paths ? o.wave_paths : (1u << 22);
         const uint64_t sets = o.wave_sets ? o.wave_sets : 3u;
-        return paths * sets * 172ull;
+        return paths * sets * ((o.flags & CRT_FLAG_OCTANT_QUEUES) ? 192ull : 136ull);
     }
 
     // ms per sample per pixel of `o`, or a negative value when the candidate
@@ -128,6 +129,16 @@ struct Tuner {
                     cur = c;
                     t = tc;
                 }
+            }
+        }
+        // octant-binned queues
+        {
+            crt_render_options c = cur;
+            c.flags ^= CRT_FLAG_OCTANT_QUEUES;
+            const float tc = measure(c);
+            if (tc > 0.f && tc < t * (1.f - kAdoptMargin)) {
+                cur = c;
+                t = tc;
             }
         }
         // scheduling: batch fetch, or lane refill at a busy-lane threshold

@@ -36,8 +36,13 @@ RenderParams make_params(crt_render r, uint32_t view, uint32_t spp0, uint32_t ns
 
 constexpr int kWaveBlock = 128;            // generate / shade / counting kernels
 constexpr int kTraversalBlockMax = 256;    // extend / shadow: block size chosen at launch
-#ifndef CRT_TRAVERSAL_MIN_BLOCKS
-#define CRT_TRAVERSAL_MIN_BLOCKS 1             // resident 256-thread blocks the register budget must allow
+// Register cap of the traversal kernels: fewer registers, more resident
+// warps to hide the dependent node loads (measured: 56 beats 64, 48 and 40).
+#ifndef CRT_TRAVERSAL_REGS
+#define CRT_TRAVERSAL_REGS 56
+#endif
+#ifndef CRT_TRAVERSAL_REGS_F32
+#define CRT_TRAVERSAL_REGS_F32 64              // FP32 planes hold more live values
 #endif
 constexpr uint32_t kDefaultCapacity = 1u << 22;
 constexpr uint32_t kDefaultWaveSets = 3;
@@ -52,7 +57,9 @@ enum Counter : uint32_t {
     C_CUR = 5,          // which extension queue is current (0/1)
     C_WAVE = 6,         // wave index within the pass
     C_FETCH_CNT = 7,    // work counter of the profiling count kernels
-    C_COUNT = 8
+    C_OCT0 = 8,         // octant-binned queues: entries per octant of queue 0 (8 words)
+    C_OCT1 = 16,        //                       and of queue 1 (8 words)
+    C_COUNT = 24
 };
 
 // Profiling totals: extension rays, nodes, triangles; shadow rays, nodes, triangles.
@@ -96,7 +103,43 @@ struct WaveParams {
     uint32_t n_mats;
     uint16_t* adj_hist;         // exact roulette: [capacity][kHistMax] kd-factor materials
     bool adj_exact;
+    // octant-binned extension queues: queue q holds 8 regions of `capacity`
+    // entries, region k the paths whose next ray points into octant k
+    bool octant;
+    uint32_t capacity;
 };
+
+// Queue entries read back in region order (octant 0 first), keeping each
+// region's order.  `pre` is the prefix of the 8 region counts, in shared
+// memory; without octant binning a queue is one region.
+struct QueueView {
+    const uint32_t* q;
+    const uint32_t* pre;   // [9], or null
+    uint32_t cap;
+    CRT_D uint32_t at(uint32_t i) const {
+        if (!pre) return q[i];
+        uint32_t k = 0;
+        while (i >= pre[k + 1]) ++k;
+        return q[(size_t)k * cap + (i - pre[k])];
+    }
+};
+
+// Builds the region prefix of queue `which` in shared memory (one block).
+CRT_D QueueView queue_view(const WaveParams& W, uint32_t which, uint32_t* pre_sh) {
+    QueueView v{W.queue[which], nullptr, W.capacity};
+    if (!W.octant) return v;
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        pre_sh[0] = 0;
+        for (int k = 0; k < 8; ++k) {
+            s += W.counters[(which ? C_OCT1 : C_OCT0) + k];
+            pre_sh[k + 1] = s;
+        }
+    }
+    __syncthreads();
+    v.pre = pre_sh;
+    return v;
+}
 
 // Exact-roulette bookkeeping per path, kept in st_W.w: history length
 // (bits 0-4); history length and channel at the previous applied roulette
@@ -233,6 +276,20 @@ CRT_D uint32_t find_segment(const WaveSeg* segs, uint32_t n, uint32_t i, bool by
     return lo;
 }
 
+// Warp-aggregated append into one of 8 regions: the lanes that want region
+// `key` share one atomic on counters[key]; returns this lane's slot in it.
+CRT_D uint32_t warp_append_keyed(uint32_t* counters, bool want, uint32_t key) {
+    const uint32_t active = __activemask();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t peers = __match_any_sync(active, want ? key : 8u) & __ballot_sync(active, want);
+    uint32_t base = 0;
+    const int leader = __ffs(peers) - 1;
+    if (want && (int)lane == leader) base = atomicAdd(counters + key, __popc(peers));
+    // every lane reads its group leader's base (lanes without work read their own)
+    base = __shfl_sync(active, base, want ? leader : (int)lane);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 // Warp-aggregated append: returns the slot for this lane (if `want`).
 CRT_D uint32_t warp_append(uint32_t* counter, bool want) {
     const uint32_t active = __activemask();
@@ -273,6 +330,11 @@ __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters[cur] = n;
         W.counters[cur ^ 1u] = 0;
+        if (W.octant)   // camera rays: one region, in pixel order
+            for (int k = 0; k < 8; ++k) {
+                W.counters[(cur ? C_OCT1 : C_OCT0) + k] = k == 0 ? n : 0u;
+                W.counters[(cur ? C_OCT0 : C_OCT1) + k] = 0;
+            }
         W.counters[C_SHADOW] = 0;
         W.counters[C_FETCH_EXT] = 0;
         W.counters[C_FETCH_SHD] = 0;
@@ -329,14 +391,14 @@ CRT_D void persistent_loop(uint32_t n, uint32_t* fetch, uint32_t chunk, uint32_t
 template <bool WHOLE_LEAF, bool F32>
 struct ExtendJob {
     const WaveParams& W;
-    const uint32_t* q;
+    QueueView q;
     Stack& st;
     Traversal<false, false, WHOLE_LEAF, F32> T;
     uint32_t path = 0, rays = 0;
 
-    CRT_D ExtendJob(const WaveParams& W_, const uint32_t* q_, Stack& st_) : W(W_), q(q_), st(st_) {}
+    CRT_D ExtendJob(const WaveParams& W_, QueueView q_, Stack& st_) : W(W_), q(q_), st(st_) {}
     CRT_D void start(uint32_t i) {
-        path = q[i];
+        path = q.at(i);
         T.init(xyz(W.st_o[path]), xyz(W.st_d[path]), kEps, FLT_MAX, -1, st);
     }
     CRT_D bool step() { return T.step(W.R.S, st, nullptr); }
@@ -359,12 +421,13 @@ CRT_D uint2* stage_top_nodes(const WaveParams& W) {
 }
 
 template <bool REFILL, bool WHOLE_LEAF, bool F32, bool TOP>
-__global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) wf_extend(WaveParams W) {
+__global__ void __maxnreg__(F32 ? CRT_TRAVERSAL_REGS_F32 : CRT_TRAVERSAL_REGS) wf_extend(WaveParams W) {
     uint2* stacks = stage_top_nodes<F32, TOP>(W);
     Stack st;
     st.setup(stacks, blockDim.x, W.stack_depth, TOP ? W.top_nodes : 0u);
     const uint32_t cur = W.counters[C_CUR];
-    ExtendJob<WHOLE_LEAF, F32> job(W, W.queue[cur], st);
+    __shared__ uint32_t pre_sh[9];
+    ExtendJob<WHOLE_LEAF, F32> job(W, queue_view(W, cur, pre_sh), st);
     persistent_loop<REFILL>(W.counters[cur], &W.counters[C_FETCH_EXT], W.queue_chunk, W.refill_busy, job);
     count_rays(W.R.ray_counts, job.rays, 0);
 }
@@ -372,12 +435,17 @@ __global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) 
 // ADJ: the adjoint replay; the same bounce with gradient hooks, shared
 // memory [n_mats][6] floats.
 template <bool ADJ>
-__global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
+// Register cap of the shade kernel: measured 64 slightly ahead of uncapped.
+#ifndef CRT_SHADE_REGS
+#define CRT_SHADE_REGS 64
+#endif
+__global__ void __maxnreg__(ADJ ? CRT_SHADE_REGS + 32 : CRT_SHADE_REGS) wf_shade(WaveParams W) {
     extern __shared__ float grad_sh[];
     if (ADJ) zero_grad_block(grad_sh, W.n_mats);
     const uint32_t cur = W.counters[C_CUR];
     const uint32_t n = W.counters[cur];
-    const uint32_t* q = W.queue[cur];
+    __shared__ uint32_t pre_sh[9];
+    const QueueView q = queue_view(W, cur, pre_sh);
     uint32_t* qn = W.queue[cur ^ 1u];
     const uint32_t end = (n + 31u) & ~31u;   // whole warps stay converged for the ballots
     for (uint32_t i = blockIdx.x * kWaveBlock + threadIdx.x; i < end; i += gridDim.x * kWaveBlock) {
@@ -385,8 +453,9 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
         uint32_t path = 0;
         ShadowReq sr;
         sr.valid = false;
+        uint32_t oct = 0;
         if (i < n) {
-            path = q[i];
+            path = q.at(i);
             const float4 o = W.st_o[path], d = W.st_d[path], c = W.st_c[path], m = W.st_m[path];
             const float4 hv = W.hit[path];
             const uint32_t pixel = __float_as_uint(o.w), sample = __float_as_uint(d.w);
@@ -429,9 +498,15 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shade(WaveParams W) {
                 want_shadow = sr.valid;
             }
             store_state(W, path, ps, ray, pixel, sample, view);
+            oct = (signbit(ray.d.x) ? 1u : 0u) | (signbit(ray.d.y) ? 2u : 0u) | (signbit(ray.d.z) ? 4u : 0u);
         }
-        const uint32_t slot = warp_append(&W.counters[cur ^ 1u], alive);
-        if (alive) qn[slot] = path;
+        if (W.octant) {
+            const uint32_t slot = warp_append_keyed(&W.counters[cur ? C_OCT0 : C_OCT1], alive, oct);
+            if (alive) qn[(size_t)oct * W.capacity + slot] = path;
+        } else {
+            const uint32_t slot = warp_append(&W.counters[cur ^ 1u], alive);
+            if (alive) qn[slot] = path;
+        }
         const uint32_t ss = warp_append(&W.counters[C_SHADOW], want_shadow);
         if (want_shadow) {
             float4* e = W.shadow + 3ull * ss;
@@ -486,7 +561,7 @@ struct ShadowJob {
 // and a visible light adds d objective / d (light material ka).  Dynamic
 // shared memory: the traversal stacks, then [n_mats][6] gradient floats.
 template <bool F32>
-__global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) wf_shadow_adj(WaveParams W) {
+__global__ void __maxnreg__(F32 ? CRT_TRAVERSAL_REGS_F32 : CRT_TRAVERSAL_REGS) wf_shadow_adj(WaveParams W) {
     uint2* stacks = stage_top_nodes<F32, true>(W);
     float* grad = reinterpret_cast<float*>(stacks + (size_t)blockDim.x * W.stack_depth);
     zero_grad_block(grad, W.n_mats);
@@ -499,7 +574,7 @@ __global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) 
 }
 
 template <bool REFILL, bool WHOLE_LEAF, bool F32, bool TOP>
-__global__ void __launch_bounds__(kTraversalBlockMax, CRT_TRAVERSAL_MIN_BLOCKS) wf_shadow(WaveParams W) {
+__global__ void __maxnreg__(F32 ? CRT_TRAVERSAL_REGS_F32 : CRT_TRAVERSAL_REGS) wf_shadow(WaveParams W) {
     uint2* stacks = stage_top_nodes<F32, TOP>(W);
     Stack st;
     st.setup(stacks, blockDim.x, W.stack_depth, TOP ? W.top_nodes : 0u);
@@ -539,6 +614,14 @@ static WaveKernel shadow_kernel(uint32_t flags, bool f32, bool top) {
 __global__ void wf_flip(WaveParams W) {
     const uint32_t cur = W.counters[C_CUR];
     W.counters[cur] = 0;
+    if (W.octant) {
+        uint32_t total = 0;
+        for (int k = 0; k < 8; ++k) {
+            W.counters[(cur ? C_OCT1 : C_OCT0) + k] = 0;
+            total += W.counters[(cur ? C_OCT0 : C_OCT1) + k];
+        }
+        W.counters[cur ^ 1u] = total;
+    }
     W.counters[C_CUR] = cur ^ 1u;
     W.counters[C_SHADOW] = 0;
     W.counters[C_FETCH_EXT] = 0;
@@ -588,6 +671,8 @@ __global__ void __launch_bounds__(kWaveBlock) wf_extend_count(WaveParams W) {
     st.setup(stack_sh, kWaveBlock, kStackShared);
     const uint32_t cur = W.counters[C_CUR];
     const uint32_t n = W.counters[cur];
+    __shared__ uint32_t pre_sh[9];
+    const QueueView q = queue_view(W, cur, pre_sh);
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t rays = 0;
     TraversalStats ts{0, 0};
@@ -598,7 +683,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_extend_count(WaveParams W) {
         if (base >= n) break;
         const uint32_t i = base + lane;
         if (i < n) {
-            const uint32_t path = W.queue[cur][i];
+            const uint32_t path = q.at(i);
             Hit h;
             h.t = FLT_MAX;
             h.face = -1;
@@ -693,17 +778,18 @@ void drop_wave_graphs(crt_render r) {
     }
 }
 
-static int alloc_set(WaveSet& S, uint32_t cap) {
+static int alloc_set(WaveSet& S, uint32_t cap, bool octant) {
     WaveBuffers& B = S.buf;
     B.capacity = cap;
+    B.octant = octant;
     const size_t c = cap;
     CRT_CUDA(B.ray_o.alloc(c * 16));
     CRT_CUDA(B.ray_d.alloc(c * 16));
     CRT_CUDA(B.color.alloc(c * 16));
     CRT_CUDA(B.mask.alloc(c * 16));
     CRT_CUDA(B.hit.alloc(c * 16));
-    CRT_CUDA(B.queue_a.alloc(c * 4));
-    CRT_CUDA(B.queue_b.alloc(c * 4));
+    CRT_CUDA(B.queue_a.alloc(c * 4 * (octant ? 8 : 1)));
+    CRT_CUDA(B.queue_b.alloc(c * 4 * (octant ? 8 : 1)));
     CRT_CUDA(B.shadow.alloc(c * 48));
     CRT_CUDA(B.counters.alloc(C_COUNT * 4));
     CRT_CUDA(cudaMemset(B.counters.p, 0, C_COUNT * 4));
@@ -719,13 +805,14 @@ static int alloc_set(WaveSet& S, uint32_t cap) {
 // `count` wave sets of the handle's capacity (reallocated when either changes).
 static int ensure_wave_sets(crt_render r, uint32_t count) {
     const uint32_t cap = r->opts.wave_paths ? r->opts.wave_paths : kDefaultCapacity;
-    if (r->sets.size() == count && r->sets[0].buf.capacity == cap) return CRT_OK;
+    const bool octant = (r->opts.flags & CRT_FLAG_OCTANT_QUEUES) != 0;
+    if (r->sets.size() == count && r->sets[0].buf.capacity == cap && r->sets[0].buf.octant == octant) return CRT_OK;
     CRT_CUDA(cudaStreamSynchronize(r->stream));
     destroy_wave_sets(r);
     CRT_CUDA(cudaEventCreateWithFlags(&r->pass_start, cudaEventDisableTiming));
     r->sets.resize(count);
     for (WaveSet& s : r->sets) {
-        int st = alloc_set(s, cap);
+        int st = alloc_set(s, cap, octant);
         if (st != CRT_OK) {
             destroy_wave_sets(r);
             return st;
@@ -769,6 +856,8 @@ static WaveParams wave_params(crt_render r, WaveSet& set) {
     W.queue_chunk = queue_chunk(r->opts);
     W.top_nodes = staged_nodes(r->scene, r->opts);
     W.refill_busy = refill_busy(r->opts);
+    W.octant = B.octant;
+    W.capacity = B.capacity;
     return W;
 }
 
@@ -1232,13 +1321,13 @@ constexpr size_t kNoAllocOff[] = {
     84ull * kNoAllocPaths,              // queue 1
     88ull * kNoAllocPaths,              // shadow requests 48 B per path
     136ull * kNoAllocPaths,             // counters (C_COUNT words)
-    136ull * kNoAllocPaths + 64,        // wave descriptor (uint4)
-    136ull * kNoAllocPaths + 96,        // its one segment (WaveSeg)
-    136ull * kNoAllocPaths + 128,       // ray counts (2 x u64)
+    136ull * kNoAllocPaths + 128,       // wave descriptor (uint4)
+    136ull * kNoAllocPaths + 160,       // its one segment (WaveSeg)
+    136ull * kNoAllocPaths + 192,       // ray counts (2 x u64)
     136ull * kNoAllocPaths + 256,       // the view (DevView)
 };
 constexpr size_t kNoAllocBytes = 136ull * kNoAllocPaths + 512;
-static_assert(sizeof(WaveSeg) == 32 && sizeof(DevView) <= 256, "no-alloc scratch layout");
+static_assert(sizeof(WaveSeg) == 32 && sizeof(DevView) <= 256 && C_COUNT * 4 <= 128, "no-alloc scratch layout");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -1332,6 +1421,8 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     W.queue_chunk = queue_chunk(o);
     W.top_nodes = staged_nodes(scene, o);
     W.refill_busy = refill_busy(o);
+    W.octant = false;   // the scratch holds single-region queues
+    W.capacity = kNoAllocPaths;
     const WaveGrids G = wave_grids(kNoAllocPaths, o.flags, f32, traversal_block(o), W.stack_depth, W.top_nodes);
     cudaStream_t s = (cudaStream_t)stream;
     DevView view;

@@ -118,3 +118,18 @@ def test_renderer_shim_compiles_against_the_reference_headers():
         pytest.skip("reference sources not present")
     res = subprocess.run(["make", "-C", shim, "check"], capture_output=True, text=True)
     assert res.returncode == 0, res.stdout + res.stderr
+
+
+def test_header_is_valid_c_and_links():
+    """include/crt_gb300.h compiles as C11 and a C host links against the
+    library (running it needs a GPU: tests/test_gpu_c_host.py)."""
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    import tempfile
+    pkg = os.path.join(ROOT, "cudart_gb300")
+    with tempfile.TemporaryDirectory() as d:
+        res = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-O2", "-I", os.path.join(ROOT, "include"),
+                              os.path.join(ROOT, "tests", "c", "abi_example.c"), "-L", pkg, "-lcrt_gb300",
+                              "-o", os.path.join(d, "abi_example")], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr

@@ -105,3 +105,12 @@ def test_bad_width_is_an_error():
     from cudart_gb300 import CrtError
     with pytest.raises(CrtError):
         bvh_build_host(scenes.cornell_box().positions, width=6)
+
+
+def test_build_is_deterministic():
+    # the build splits large ranges across threads; min/max bounds and
+    # integer bin counts merge exactly, so repeated builds are identical
+    pos = scenes.large_textured(grid=256, tex_size=16, n_spheres=8, sphere_subdiv=2).positions
+    a_nodes, a_tris, _ = bvh_build_host(pos)
+    b_nodes, b_tris, _ = bvh_build_host(pos)
+    assert a_nodes.tobytes() == b_nodes.tobytes() and a_tris.tobytes() == b_tris.tobytes()

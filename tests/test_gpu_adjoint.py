@@ -131,6 +131,19 @@ def test_exact_roulette_adjoint_matches_finite_differences(cuda):
         assert abs(np.median(diffs)) <= 0.02, (key, diffs)
 
 
+def test_octant_queues_give_the_same_gradient(cuda):
+    sc = scenes.material_inversion(width=64, height=64)
+    adj = _adjoint_image(sc)
+    g = GB300Scene(sc)
+    out = []
+    for flags in (0, 4):
+        r = GB300Renderer(g, sc.width, sc.height, 8, max_depth=6, seed=2, mode="wavefront", flags=flags,
+                          wave_paths=1 << 16)
+        out.append(_gpu_adjoint(cuda, r, len(sc.materials), adj, 0, 8))
+    for a, b in zip(out[0], out[1]):   # the atomics' order differs: FP32 rounding only
+        assert np.allclose(a, b, rtol=1e-4, atol=1e-6 * np.abs(a).max())
+
+
 def test_torch_autograd_wrapper(cuda):
     torch = cuda
     sc = scenes.material_inversion(width=64, height=64)

@@ -43,7 +43,7 @@ def test_wavefront_equals_megakernel(cuda):
     assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("flags", [1, 2, 3])
+@pytest.mark.parametrize("flags", [1, 2, 3, 4, 5])
 def test_scheduling_flags_do_not_change_results(cuda, flags):
     sc = scenes.cornell_box(width=96, height=64)
     a = _render(sc, 8, 5, "wavefront", wave_paths=1 << 15).accum()
