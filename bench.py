@@ -406,9 +406,10 @@ def run_gb300(args):
         traffic = None
         tp = os.path.join(ROOT, "profiles", "traffic_per_ray.json")
         if os.path.exists(tp):
-            tr = json.load(open(tp)).get(main["kernel"])
+            fmt = "f32" if wf.options.node_format == 1 else "q8"
+            tr = json.load(open(tp)).get(main["kernel"], {}).get(fmt)
             if tr:
-                traffic = tr["dram_bytes_per_ray"] * main["rays"] / prof[f"{dom if dom in roof else 'extend'}_launches"]
+                traffic = round(tr["dram_bytes_per_ray"] * main["rays"] / prof[f"{dom if dom in roof else 'extend'}_launches"])
         roofline = {"bound": "hbm", "kernel": main["kernel"], "achieved": round(main["gbs"], 1),
                     "peak": peak, "unit": "GB/s", "frac": round(main["gbs"] / peak, 4),
                     "traffic": traffic, "peak_kind": f"{peak_kind} (HBM copy)",

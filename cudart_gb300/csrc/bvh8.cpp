@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <future>
+#include <memory>
 #include <mutex>
 #include <thread>
 
@@ -32,11 +33,12 @@ struct Box {
 
 struct Node2 {
     Box box;
-    int32_t left = -1, right = -1;   // children (internal)
-    uint32_t first = 0, count = 0;   // leaf range into the index array (count > 0)
+    int32_t left, right;     // children (internal)
+    uint32_t first, count;   // leaf range into the index array (count > 0)
 };
 
 constexpr int kBins = 32;
+constexpr uint32_t kSmallMax = 32;        // ranges up to this size get an exact SAH sweep
 constexpr uint32_t kLeafMax = 3;          // the reference's maxTrisInNode (bvh.cpp:62)
 constexpr uint32_t kParallelMin = 1u << 15;
 
@@ -86,7 +88,49 @@ struct Builder {
     // Binned SAH split of idx[start, end); returns mid (start < mid < end).
     // Large ranges are binned by several threads; boxes merge by min / max
     // and counts by sums, so the split does not depend on the thread count.
+    // Exact SAH split of a small range: per axis, sort by centroid and sweep
+    // every split position (cheaper than 32 bins per axis, and exact).
+    uint32_t split_small(uint32_t start, uint32_t end) const {
+        const uint32_t n = end - start;
+        uint32_t order[3][kSmallMax];
+        float right_area[kSmallMax];
+        float best_cost = FLT_MAX;
+        int best_axis = -1;
+        uint32_t best_pos = 0;
+        for (int ax = 0; ax < 3; ++ax) {
+            uint32_t* o = order[ax];
+            for (uint32_t i = 0; i < n; ++i) o[i] = idx[start + i];
+            // insertion sort by centroid, ties by triangle index (deterministic)
+            for (uint32_t i = 1; i < n; ++i) {
+                const uint32_t t = o[i];
+                const float c = cent[3 * t + ax];
+                uint32_t j = i;
+                while (j > 0 && (cent[3 * o[j - 1] + ax] > c || (cent[3 * o[j - 1] + ax] == c && o[j - 1] > t))) {
+                    o[j] = o[j - 1];
+                    --j;
+                }
+                o[j] = t;
+            }
+            Box acc;
+            acc.reset();
+            for (uint32_t i = n; i-- > 1;) {
+                acc.grow(tbox[o[i]]);
+                right_area[i] = acc.half_area();
+            }
+            acc.reset();
+            for (uint32_t i = 1; i < n; ++i) {
+                acc.grow(tbox[o[i - 1]]);
+                const float cost = acc.half_area() * i + right_area[i] * (n - i);
+                if (cost < best_cost) { best_cost = cost; best_axis = ax; best_pos = i; }
+            }
+        }
+        if (best_axis < 0) return start + n / 2;
+        for (uint32_t i = 0; i < n; ++i) idx[start + i] = order[best_axis][i];
+        return start + best_pos;
+    }
+
     uint32_t split(uint32_t start, uint32_t end, const Box& cb) const {
+        if (end - start <= kSmallMax) return split_small(start, end);
         float scale[3];
         for (int ax = 0; ax < 3; ++ax) {
             const float ext = cb.hi[ax] - cb.lo[ax];
@@ -149,7 +193,6 @@ struct Builder {
         return m;
     }
 
-    // Builds idx[start, end) into `out`; returns the subtree root index.
     // Bounds of the triangles and of the centroids of idx[s, e).
     void bounds(uint32_t s, uint32_t e, Box& nb, Box& cb) const {
         for (uint32_t i = s; i < e; ++i) {
@@ -162,7 +205,10 @@ struct Builder {
         }
     }
 
-    int32_t build(uint32_t start, uint32_t end, std::vector<Node2>& out, int par_depth) const {
+    // Builds idx[start, end) at nodes[slot]: a subtree of m primitives owns
+    // slots [slot, slot + 2m - 1) (a binary tree has at most 2m - 1 nodes),
+    // so subtrees built in parallel write disjoint ranges of one array.
+    void build(uint32_t start, uint32_t end, Node2* nodes, uint32_t slot, int par_depth) const {
         Box nb, cb;
         nb.reset();
         cb.reset();
@@ -185,40 +231,28 @@ struct Builder {
         } else {
             bounds(start, end, nb, cb);
         }
-        int32_t me = (int32_t)out.size();
-        out.emplace_back();
-        out[me].box = nb;
+        Node2& me = nodes[slot];
+        me.box = nb;
         if (end - start <= kLeafMax) {
-            out[me].first = start;
-            out[me].count = end - start;
-            return me;
+            me.left = me.right = -1;
+            me.first = start;
+            me.count = end - start;
+            return;
         }
-        uint32_t mid = split(start, end, cb);
+        const uint32_t mid = split(start, end, cb);
+        const uint32_t lslot = slot + 1, rslot = slot + 2 * (mid - start);
+        me.left = (int32_t)lslot;
+        me.right = (int32_t)rslot;
+        me.first = 0;
+        me.count = 0;
         if (par_depth > 0 && end - start >= kParallelMin) {
-            std::vector<Node2> lv;
-            auto fut = std::async(std::launch::async, [&] { return build(start, mid, lv, par_depth - 1); });
-            std::vector<Node2> rv;
-            int32_t rr = build(mid, end, rv, par_depth - 1);
-            int32_t lr = fut.get();
-            int32_t lbase = (int32_t)out.size();
-            for (Node2 n : lv) {
-                if (n.count == 0) { n.left += lbase; n.right += lbase; }
-                out.push_back(n);
-            }
-            int32_t rbase = (int32_t)out.size();
-            for (Node2 n : rv) {
-                if (n.count == 0) { n.left += rbase; n.right += rbase; }
-                out.push_back(n);
-            }
-            out[me].left = lbase + lr;
-            out[me].right = rbase + rr;
+            auto fut = std::async(std::launch::async, [&] { build(start, mid, nodes, lslot, par_depth - 1); });
+            build(mid, end, nodes, rslot, par_depth - 1);
+            fut.get();
         } else {
-            int32_t l = build(start, mid, out, 0);
-            int32_t r = build(mid, end, out, 0);
-            out[me].left = l;
-            out[me].right = r;
+            build(start, mid, nodes, lslot, 0);
+            build(mid, end, nodes, rslot, 0);
         }
-        return me;
     }
 };
 
@@ -289,12 +323,13 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
     std::vector<uint32_t> idx(n);
     for (uint32_t i = 0; i < n; ++i) idx[i] = i;
     Builder b{tbox.data(), cent.data(), idx.data(), std::max(1u, std::thread::hardware_concurrency())};
-    std::vector<Node2> n2;
-    n2.reserve(2ull * n);
+    std::unique_ptr<Node2[]> n2_store(new Node2[2ull * n - 1]);   // slots, see Builder::build
+    const Node2* n2 = n2_store.get();
     unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     int par_depth = 0;
     while ((1u << par_depth) < hw * 2 && par_depth < 8) ++par_depth;
-    int32_t root = b.build(0, n, n2, par_depth);
+    b.build(0, n, n2_store.get(), 0, par_depth);
+    const int32_t root = 0;
 
     // ---- collapse to max_children-wide nodes, breadth-first layout --------
     // 1. (serial, cheap) each wide node takes its BVH2 node's children and

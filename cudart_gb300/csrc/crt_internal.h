@@ -133,7 +133,7 @@ inline bool uses_f32_nodes(const crt_render_s* r) { return uses_f32_nodes(r->sce
 
 // Traversal launch shape of a wavefront render.
 inline uint32_t traversal_block(const crt_render_options& o) { return o.block_size ? o.block_size : 128u; }
-inline uint32_t traversal_stack(const crt_render_options& o) { return o.stack_depth ? o.stack_depth : 16u; }
+inline uint32_t traversal_stack(const crt_render_options& o) { return o.stack_depth ? o.stack_depth : 8u; }
 inline uint32_t queue_chunk(const crt_render_options& o) { return o.queue_chunk ? o.queue_chunk : 32u; }
 inline uint32_t refill_busy(const crt_render_options& o) { return o.refill_busy ? o.refill_busy : 31u; }
 inline uint32_t staged_nodes(const crt_scene_s* s, const crt_render_options& o) {

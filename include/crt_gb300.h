@@ -246,7 +246,7 @@ typedef struct {
     uint32_t wave_sets;        /* wavefront: waves in flight at once, each with its
                                   own buffers and stream, 0..8 (0 = default 3) */
     uint32_t stack_depth;      /* wavefront traversal kernels: stack entries per
-                                  thread kept in shared memory, 4..32 (0 = 16);
+                                  thread kept in shared memory, 4..32 (0 = 8);
                                   deeper entries go to local memory */
     int32_t node_format;       /* crt_node_format, or -1 for the scene's format */
     uint32_t queue_chunk;      /* wavefront traversal kernels: queue entries a warp
