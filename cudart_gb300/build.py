@@ -24,7 +24,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["scene.cu", "trace.cu", "render.cu", "wavefront.cu", "tune.cu"]
+CU_SOURCES = ["scene.cu", "trace.cu", "render.cu", "wavefront.cu", "tune.cu", "bvh_gpu.cu"]
 CPP_SOURCES = ["bvh8.cpp"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",

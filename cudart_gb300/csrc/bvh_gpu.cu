@@ -1,0 +1,512 @@
+// bvh_gpu.cu -- GPU build of the 8-wide (or 4-wide) quantised BVH.
+//
+// A linear BVH over 30-bit Morton codes of the triangle centroids (Karras,
+// "Maximizing parallelism in the construction of BVHs, octrees, and k-d
+// trees", HPG 2012), subtree boxes bottom-up, then the host build's
+// collapse and encoding (bvh8.cpp) run level by level: each wide node opens
+// its largest-area internal children until it has 8 (or 4), assigns them to
+// slots by octant, and quantises their boxes outward on a power-of-two grid.
+// A subtree of at most 3 triangles becomes a leaf slot (the reference's leaf
+// size, bvh.cpp:62).  Node and triangle layouts are the host build's, so the
+// traversal kernels and every query result are unchanged; only the tree
+// differs, and with it the number of nodes a ray visits.
+//
+// Triangle boxes get the host build's conservative margin (2^-15 of the
+// largest coordinate magnitude, computed in FP64 and rounded outward).
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <chrono>
+#include <vector>
+
+#include "crt_internal.h"
+
+namespace crt {
+namespace {
+
+constexpr uint32_t kLeafMaxGpu = 3;
+constexpr int kBlock = 256;
+
+struct GBox {
+    float lo[3], hi[3];
+};
+
+// Binary nodes: internal k at index k (0..n-2), triangle i (sorted order) at
+// n-1+i.  [first, first+count) is the node's range of sorted triangles.
+struct GNode {
+    GBox box;
+    int32_t left, right, parent;
+    uint32_t first, count;
+};
+
+// Children of one wide node, in the order the collapse picked them.
+struct GWide {
+    int32_t nch;
+    int32_t ch[8];
+    int32_t slot_of[8];
+};
+
+__device__ __forceinline__ uint32_t float_order(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float order_float(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+__device__ __forceinline__ float half_area(const GBox& b) {
+    const float dx = fmaxf(b.hi[0] - b.lo[0], 0.f), dy = fmaxf(b.hi[1] - b.lo[1], 0.f),
+                dz = fmaxf(b.hi[2] - b.lo[2], 0.f);
+    return dx * dy + dy * dz + dz * dx;
+}
+__device__ __forceinline__ void grow(GBox& a, const GBox& b) {
+    for (int k = 0; k < 3; ++k) {
+        a.lo[k] = fminf(a.lo[k], b.lo[k]);
+        a.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+    }
+}
+
+// Largest coordinate magnitude, as order-preserving bits of a positive float.
+__global__ void k_max_abs(const float* __restrict__ v1, const float* __restrict__ e1, const float* __restrict__ e2,
+                          uint32_t n3, uint32_t* out) {
+    float m = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        const float a = v1[i];
+        m = fmaxf(m, fmaxf(fabsf(a), fmaxf(fabsf(a + e1[i]), fabsf(a + e2[i]))));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if ((threadIdx.x & 31u) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// Conservative triangle boxes and centroids exactly as the host build forms
+// them (FP64 bounds minus / plus the margin, rounded outward to FP32), and
+// the centroid bounds.
+__global__ void k_tri_boxes(const float* __restrict__ v1, const float* __restrict__ e1, const float* __restrict__ e2,
+                            uint32_t n, float margin, GBox* __restrict__ tbox, float* __restrict__ cent,
+                            uint32_t* __restrict__ cbounds) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        GBox b;
+        for (int k = 0; k < 3; ++k) {
+            const double a = v1[3ull * t + k];
+            const double bb = a + (double)e1[3ull * t + k];
+            const double c = a + (double)e2[3ull * t + k];
+            const double lo = fmin(a, fmin(bb, c)) - (double)margin, hi = fmax(a, fmax(bb, c)) + (double)margin;
+            float flo = __double2float_rn(lo), fhi = __double2float_rn(hi);
+            if ((double)flo > lo) flo = nextafterf(flo, -FLT_MAX);
+            if ((double)fhi < hi) fhi = nextafterf(fhi, FLT_MAX);
+            b.lo[k] = flo;
+            b.hi[k] = fhi;
+            const float cc = 0.5f * (flo + fhi);
+            cent[3ull * t + k] = cc;
+            atomicMin(&cbounds[k], float_order(cc));
+            atomicMax(&cbounds[3 + k], float_order(cc));
+        }
+        tbox[t] = b;
+    }
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__global__ void k_morton(const float* __restrict__ cent, uint32_t n, const uint32_t* __restrict__ cbounds,
+                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    float lo[3], sc[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = order_float(cbounds[k]);
+        const float ext = order_float(cbounds[3 + k]) - lo[k];
+        sc[k] = ext > 0.f ? 1023.f / ext : 0.f;
+    }
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+            const float f = (cent[3ull * t + k] - lo[k]) * sc[k];
+            q[k] = (uint32_t)fminf(fmaxf(f, 0.f), 1023.f);
+        }
+        keys[t] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+        vals[t] = t;
+    }
+}
+
+// Length of the common prefix of sorted keys a and b (index order breaks ties).
+__device__ __forceinline__ int delta(const uint32_t* keys, int n, int a, int b) {
+    if (b < 0 || b >= n) return -1;
+    const uint32_t ka = keys[a], kb = keys[b];
+    if (ka == kb) return 32 + __clz((uint32_t)(a ^ b));
+    return __clz(ka ^ kb);
+}
+
+__global__ void k_karras(const uint32_t* __restrict__ keys, int n, GNode* __restrict__ nodes, uint32_t* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = delta(keys, n, i, i + 1) > delta(keys, n, i, i - 1) ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = delta(keys, n, i, j);
+    int s = 0;
+    for (int t = (l + 1) / 2;; t = (t + 1) / 2) {
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t == 1) break;
+    }
+    const int gamma = i + s * d + min(d, 0);
+    const int first = min(i, j), last = max(i, j);
+    const int left = (first == gamma) ? (n - 1 + gamma) : gamma;
+    const int right = (last == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+    if (gamma < first || gamma + 1 > last || left <= 0 || right <= 0 || left > 2 * n - 2 || right > 2 * n - 2) {
+        atomicOr(err, 1u);   // never expected; keeps every write in bounds
+        return;
+    }
+    GNode& me = nodes[i];
+    me.left = left;
+    me.right = right;
+    me.first = (uint32_t)first;
+    me.count = (uint32_t)(last - first + 1);
+    nodes[left].parent = i;
+    nodes[right].parent = i;
+}
+
+__global__ void k_leaves(const GBox* __restrict__ tbox, const uint32_t* __restrict__ perm, int n,
+                         GNode* __restrict__ nodes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    GNode& lf = nodes[n - 1 + i];
+    lf.box = tbox[perm[i]];
+    lf.left = lf.right = -1;
+    lf.first = (uint32_t)i;
+    lf.count = 1;
+}
+
+// Boxes of the internal nodes: the second child to finish computes the parent.
+__global__ void k_bottom_up(int n, GNode* nodes, uint32_t* flags, uint32_t* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = nodes[n - 1 + i].parent;
+    for (int climbed = 0; p >= 0; ++climbed) {
+        if (p > n - 2 || climbed >= n) {   // never expected; ends the climb
+            atomicOr(err, 8u);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[p], 1u) == 0) return;   // the sibling subtree is not done yet
+        __threadfence();
+        const int l = __ldcg(&nodes[p].left), r = __ldcg(&nodes[p].right);
+        GBox b;
+        for (int k = 0; k < 3; ++k) {
+            b.lo[k] = fminf(__ldcg(&nodes[l].box.lo[k]), __ldcg(&nodes[r].box.lo[k]));
+            b.hi[k] = fmaxf(__ldcg(&nodes[l].box.hi[k]), __ldcg(&nodes[r].box.hi[k]));
+        }
+        __stcg(&nodes[p].box.lo[0], b.lo[0]);
+        __stcg(&nodes[p].box.lo[1], b.lo[1]);
+        __stcg(&nodes[p].box.lo[2], b.lo[2]);
+        __stcg(&nodes[p].box.hi[0], b.hi[0]);
+        __stcg(&nodes[p].box.hi[1], b.hi[1]);
+        __stcg(&nodes[p].box.hi[2], b.hi[2]);
+        p = __ldcg(&nodes[p].parent);
+    }
+}
+
+__device__ __forceinline__ bool opens(const GNode& nd) { return nd.count > kLeafMaxGpu; }
+
+// One wide node per thread: children by largest area, slots by octant.
+__global__ void k_choose(const int32_t* __restrict__ front, uint32_t F, const GNode* __restrict__ nodes,
+                         int max_children, GWide* __restrict__ recs, uint32_t* __restrict__ cnt_int,
+                         uint32_t* __restrict__ cnt_tri) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    const int32_t x = front[f];
+    GWide w;
+    int nch = 0;
+    if (!opens(nodes[x])) {
+        w.ch[nch++] = x;                      // a root of at most 3 triangles
+    } else {
+        w.ch[nch++] = nodes[x].left;
+        w.ch[nch++] = nodes[x].right;
+        while (nch < max_children) {
+            int best = -1;
+            float area = -1.f;
+            for (int c = 0; c < nch; ++c)
+                if (opens(nodes[w.ch[c]]) && half_area(nodes[w.ch[c]].box) > area) {
+                    area = half_area(nodes[w.ch[c]].box);
+                    best = c;
+                }
+            if (best < 0) break;
+            const int32_t y = w.ch[best];
+            w.ch[best] = nodes[y].left;
+            w.ch[nch++] = nodes[y].right;
+        }
+    }
+    w.nch = nch;
+    GBox nb;
+    for (int k = 0; k < 3; ++k) { nb.lo[k] = FLT_MAX; nb.hi[k] = -FLT_MAX; }
+    for (int c = 0; c < nch; ++c) grow(nb, nodes[w.ch[c]].box);
+    float pc[3];
+    for (int k = 0; k < 3; ++k) pc[k] = 0.5f * (nb.lo[k] + nb.hi[k]);
+    bool used_slot[8] = {false, false, false, false, false, false, false, false};
+    bool placed[8] = {false, false, false, false, false, false, false, false};
+    for (int round = 0; round < nch; ++round) {
+        float best = -FLT_MAX;
+        int bc = -1, bs = -1;
+        for (int c = 0; c < nch; ++c) {
+            if (placed[c]) continue;
+            const GBox& cb = nodes[w.ch[c]].box;
+            float dd[3];
+            for (int k = 0; k < 3; ++k) dd[k] = 0.5f * (cb.lo[k] + cb.hi[k]) - pc[k];
+            for (int s = 0; s < 8; ++s) {
+                if (used_slot[s]) continue;
+                const float sc = ((s & 1) ? dd[0] : -dd[0]) + ((s & 2) ? dd[1] : -dd[1]) + ((s & 4) ? dd[2] : -dd[2]);
+                if (sc > best) { best = sc; bc = c; bs = s; }
+            }
+        }
+        placed[bc] = true;
+        used_slot[bs] = true;
+        w.slot_of[bc] = bs;
+    }
+    uint32_t ni = 0, nt = 0;
+    for (int c = 0; c < nch; ++c) {
+        if (opens(nodes[w.ch[c]])) ++ni;
+        else nt += nodes[w.ch[c]].count;
+    }
+    recs[f] = w;
+    cnt_int[f] = ni;
+    cnt_tri[f] = nt;
+}
+
+__device__ int scale_exponent_d(double ext) {
+    if (!(ext > 0.0)) return -126;
+    int k;
+    const double m = frexp(ext / 255.0, &k);
+    const int e = (m == 0.5) ? k - 1 : k;
+    return max(-126, min(127, e));
+}
+
+// Encodes the wide nodes of one level (the host build's encoding), writes
+// the next level's frontier and the triangle records of the leaf slots.
+__global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t level_base, uint32_t next_base,
+                       uint32_t tri_level_base, const uint32_t* __restrict__ int_off,
+                       const uint32_t* __restrict__ tri_off, const GNode* __restrict__ nodes,
+                       const uint32_t* __restrict__ perm, const float* __restrict__ v1,
+                       const float* __restrict__ e1, const float* __restrict__ e2, Bvh8Node* __restrict__ out,
+                       Bvh8FloatNode* __restrict__ fout, TriRecord* __restrict__ tris, int32_t* __restrict__ next_front,
+                       uint32_t n_tris, uint32_t cap_nodes, uint32_t* err) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    if (level_base + f >= cap_nodes) {
+        atomicOr(err, 2u);
+        return;
+    }
+    const GWide w = recs[f];
+    int child_at[8];
+    for (int s = 0; s < 8; ++s) child_at[s] = -1;
+    for (int c = 0; c < w.nch; ++c) child_at[w.slot_of[c]] = c;
+    GBox nb;
+    for (int k = 0; k < 3; ++k) { nb.lo[k] = FLT_MAX; nb.hi[k] = -FLT_MAX; }
+    for (int c = 0; c < w.nch; ++c) grow(nb, nodes[w.ch[c]].box);
+    Bvh8Node node;
+    memset(&node, 0, sizeof(node));
+    Bvh8FloatNode fnode;
+    memset(&fnode, 0, sizeof(fnode));
+    node.px = nb.lo[0];
+    node.py = nb.lo[1];
+    node.pz = nb.lo[2];
+    int e[3];
+    for (int k = 0; k < 3; ++k) e[k] = scale_exponent_d((double)nb.hi[k] - (double)nb.lo[k]);
+    node.ex = (uint8_t)(e[0] + 127);
+    node.ey = (uint8_t)(e[1] + 127);
+    node.ez = (uint8_t)(e[2] + 127);
+    node.child_base = next_base + int_off[f];
+    node.tri_base = tri_level_base + tri_off[f];
+    uint32_t tri_o = 0, int_o = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int c = child_at[s];
+        if (c < 0) {
+            for (int k = 0; k < 3; ++k) {
+                node.qlo[k][s] = 255;
+                node.qhi[k][s] = 0;
+                fnode.lo[k][s] = FLT_MAX;
+                fnode.hi[k][s] = -FLT_MAX;
+            }
+            continue;
+        }
+        const GNode& cn = nodes[w.ch[c]];
+        for (int k = 0; k < 3; ++k) {
+            fnode.lo[k][s] = cn.box.lo[k];
+            fnode.hi[k][s] = cn.box.hi[k];
+            const double step = ldexp(1.0, e[k]);
+            const double lo = floor(((double)cn.box.lo[k] - (double)nb.lo[k]) / step);
+            const double hi = ceil(((double)cn.box.hi[k] - (double)nb.lo[k]) / step);
+            node.qlo[k][s] = (uint8_t)fmax(0.0, fmin(255.0, lo));
+            node.qhi[k][s] = (uint8_t)fmax(0.0, fmin(255.0, hi));
+        }
+        if (opens(cn)) {
+            node.imask |= (uint8_t)(1u << s);
+            node.meta[s] = 0x80;
+            const uint32_t k = int_off[f] + int_o++;
+            if (next_base + k < cap_nodes) next_front[k] = w.ch[c];
+            else atomicOr(err, 2u);
+        } else {
+            node.meta[s] = (uint8_t)((cn.count << 5) | tri_o);
+            for (uint32_t i = 0; i < cn.count; ++i) {
+                const uint32_t t = perm[cn.first + i];
+                TriRecord r;
+                for (int k = 0; k < 3; ++k) {
+                    r.v1[k] = v1[3ull * t + k];
+                    r.e1[k] = e1[3ull * t + k];
+                    r.e2[k] = e2[3ull * t + k];
+                }
+                r.face = t;
+                r.pad1 = r.pad2 = 0.f;
+                if (node.tri_base + tri_o + i < n_tris) tris[node.tri_base + tri_o + i] = r;
+                else atomicOr(err, 4u);
+            }
+            tri_o += cn.count;
+        }
+    }
+    out[level_base + f] = node;
+    fnode.child_base_imask = node.child_base | ((uint32_t)node.imask << 24);
+    fnode.tri_base = node.tri_base;
+    memcpy(fnode.meta, node.meta, 8);
+    fout[level_base + f] = fnode;
+}
+
+uint32_t blocks(uint64_t n) { return (uint32_t)std::max<uint64_t>(1, (n + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+// Builds the BVH of n triangles (device arrays v1/e1/e2, [n][3]) into nodes,
+// fnodes and tris (device, allocated here); fills max_depth and the node
+// count.  Returns CRT_OK or an error with its message set.
+int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint32_t n, uint32_t max_levels,
+                  int max_children, DevBuf& nodes_out, DevBuf& fnodes_out, DevBuf& tris_out, uint32_t* num_nodes,
+                  uint32_t* max_depth, bool* fnodes_ok, cudaStream_t s) {
+    if (n == 0) return set_error(CRT_ERR_INVALID, "scene has no triangles");
+    if (n >= (1u << 30)) return set_error(CRT_ERR_LIMIT, "GPU BVH build: at most 2^30 triangles");
+    DevBuf maxbits, tbox, cent, cbounds, keys, vals, keys2, perm, gnodes, flags, tmp, errbuf;
+    CRT_CUDA(errbuf.alloc(4));
+    CRT_CUDA(cudaMemsetAsync(errbuf.p, 0, 4, s));
+    uint32_t* err = errbuf.as<uint32_t>();
+    CRT_CUDA(maxbits.alloc(4));
+    CRT_CUDA(cudaMemsetAsync(maxbits.p, 0, 4, s));
+    k_max_abs<<<blocks(3ull * n) < 1024 ? blocks(3ull * n) : 1024, kBlock, 0, s>>>(d_v1, d_e1, d_e2, 3 * n,
+                                                                                  maxbits.as<uint32_t>());
+    uint32_t mb = 0;
+    CRT_CUDA(cudaMemcpyAsync(&mb, maxbits.p, 4, cudaMemcpyDeviceToHost, s));
+    CRT_CUDA(cudaStreamSynchronize(s));
+    float maxabs;
+    std::memcpy(&maxabs, &mb, 4);
+    const float margin = (float)std::ldexp(std::max(1.0, (double)maxabs), -15);
+
+    CRT_CUDA(tbox.alloc((size_t)n * sizeof(GBox)));
+    CRT_CUDA(cent.alloc((size_t)n * 12));
+    CRT_CUDA(cbounds.alloc(24));
+    const uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    CRT_CUDA(cudaMemcpyAsync(cbounds.p, init, 24, cudaMemcpyHostToDevice, s));
+    k_tri_boxes<<<std::min<uint32_t>(blocks(n), 4096), kBlock, 0, s>>>(d_v1, d_e1, d_e2, n, margin, tbox.as<GBox>(),
+                                                                        cent.as<float>(), cbounds.as<uint32_t>());
+    CRT_CUDA(keys.alloc((size_t)n * 4));
+    CRT_CUDA(vals.alloc((size_t)n * 4));
+    CRT_CUDA(keys2.alloc((size_t)n * 4));
+    CRT_CUDA(perm.alloc((size_t)n * 4));
+    k_morton<<<std::min<uint32_t>(blocks(n), 4096), kBlock, 0, s>>>(cent.as<float>(), n, cbounds.as<uint32_t>(),
+                                                                     keys.as<uint32_t>(), vals.as<uint32_t>());
+    size_t tmp_bytes = 0;
+    CRT_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint32_t>(), keys2.as<uint32_t>(),
+                                             vals.as<uint32_t>(), perm.as<uint32_t>(), (int)n, 0, 30, s));
+    CRT_CUDA(tmp.alloc(tmp_bytes));
+    CRT_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint32_t>(), keys2.as<uint32_t>(),
+                                             vals.as<uint32_t>(), perm.as<uint32_t>(), (int)n, 0, 30, s));
+    const int ni = (int)n;
+    CRT_CUDA(gnodes.alloc((size_t)(2 * n - 1) * sizeof(GNode)));
+    CRT_CUDA(cudaMemsetAsync(gnodes.p, 0xFF, gnodes.bytes, s));   // every parent / child index starts at -1
+    GNode* gn = gnodes.as<GNode>();
+    k_leaves<<<blocks(n), kBlock, 0, s>>>(tbox.as<GBox>(), perm.as<uint32_t>(), ni, gn);
+    int32_t root = (int32_t)n - 1;   // a lone triangle is its own root
+    if (n > 1) {
+        k_karras<<<blocks(n - 1), kBlock, 0, s>>>(keys2.as<uint32_t>(), ni, gn, err);
+        const int32_t none = -1;
+        CRT_CUDA(cudaMemcpyAsync(&gn[0].parent, &none, 4, cudaMemcpyHostToDevice, s));
+        CRT_CUDA(flags.alloc((size_t)n * 4));
+        CRT_CUDA(cudaMemsetAsync(flags.p, 0, (size_t)n * 4, s));
+        k_bottom_up<<<blocks(n), kBlock, 0, s>>>(ni, gn, flags.as<uint32_t>(), err);
+        root = 0;
+    } else {
+        const int32_t none = -1;
+        CRT_CUDA(cudaMemcpyAsync(&gn[0].parent, &none, 4, cudaMemcpyHostToDevice, s));
+    }
+    CRT_CUDA(cudaGetLastError());
+    {   // the collapse follows child links: stop here if any were not set
+        uint32_t e = 0;
+        CRT_CUDA(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s));
+        CRT_CUDA(cudaStreamSynchronize(s));
+        if (e) return set_error(CRT_ERR_CUDA, "GPU BVH build: inconsistent hierarchy (" + std::to_string(e) + ")");
+    }
+
+    // ---- collapse level by level -------------------------------------------
+    const uint32_t cap_nodes = n;   // a wide node holds >= 1 triangle of its own subtree
+    CRT_CUDA(nodes_out.alloc((size_t)cap_nodes * sizeof(Bvh8Node)));
+    CRT_CUDA(fnodes_out.alloc((size_t)cap_nodes * sizeof(Bvh8FloatNode)));
+    CRT_CUDA(tris_out.alloc((size_t)n * sizeof(TriRecord)));
+    DevBuf front_a, front_b, recs, cnt_int, cnt_tri, off_int, off_tri, scan_tmp;
+    CRT_CUDA(front_a.alloc((size_t)cap_nodes * 4));
+    CRT_CUDA(front_b.alloc((size_t)cap_nodes * 4));
+    CRT_CUDA(recs.alloc((size_t)cap_nodes * sizeof(GWide)));
+    CRT_CUDA(cnt_int.alloc((size_t)cap_nodes * 4 + 4));
+    CRT_CUDA(cnt_tri.alloc((size_t)cap_nodes * 4 + 4));
+    CRT_CUDA(off_int.alloc((size_t)cap_nodes * 4 + 4));
+    CRT_CUDA(off_tri.alloc((size_t)cap_nodes * 4 + 4));
+    size_t scan_bytes = 0;
+    CRT_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, cnt_int.as<uint32_t>(), off_int.as<uint32_t>(),
+                                           (int)cap_nodes + 1, s));
+    CRT_CUDA(scan_tmp.alloc(scan_bytes));
+    CRT_CUDA(cudaMemcpyAsync(front_a.p, &root, 4, cudaMemcpyHostToDevice, s));
+    uint32_t F = 1, level_base = 0, tri_base = 0, depth = 0;
+    int32_t* cur = front_a.as<int32_t>();
+    int32_t* nxt = front_b.as<int32_t>();
+    while (F > 0) {
+        if (++depth > max_levels) return set_error(CRT_ERR_LIMIT, "BVH deeper than the traversal stack allows");
+        k_choose<<<blocks(F), kBlock, 0, s>>>(cur, F, gn, max_children, recs.as<GWide>(), cnt_int.as<uint32_t>(),
+                                              cnt_tri.as<uint32_t>());
+        // exclusive sums over F + 1 entries: the last is each level's total
+        CRT_CUDA(cudaMemsetAsync(cnt_int.as<uint32_t>() + F, 0, 4, s));
+        CRT_CUDA(cudaMemsetAsync(cnt_tri.as<uint32_t>() + F, 0, 4, s));
+        CRT_CUDA(cub::DeviceScan::ExclusiveSum(scan_tmp.p, scan_bytes, cnt_int.as<uint32_t>(), off_int.as<uint32_t>(),
+                                               (int)F + 1, s));
+        CRT_CUDA(cub::DeviceScan::ExclusiveSum(scan_tmp.p, scan_bytes, cnt_tri.as<uint32_t>(), off_tri.as<uint32_t>(),
+                                               (int)F + 1, s));
+        const uint32_t next_base = level_base + F;
+        k_emit<<<blocks(F), kBlock, 0, s>>>(recs.as<GWide>(), F, level_base, next_base, tri_base,
+                                            off_int.as<uint32_t>(), off_tri.as<uint32_t>(), gn, perm.as<uint32_t>(),
+                                            d_v1, d_e1, d_e2, nodes_out.as<Bvh8Node>(), fnodes_out.as<Bvh8FloatNode>(),
+                                            tris_out.as<TriRecord>(), nxt, n, cap_nodes, err);
+        uint32_t totals[2];
+        CRT_CUDA(cudaMemcpyAsync(&totals[0], off_int.as<uint32_t>() + F, 4, cudaMemcpyDeviceToHost, s));
+        CRT_CUDA(cudaMemcpyAsync(&totals[1], off_tri.as<uint32_t>() + F, 4, cudaMemcpyDeviceToHost, s));
+        CRT_CUDA(cudaStreamSynchronize(s));
+        CRT_CUDA(cudaGetLastError());
+        level_base = next_base;
+        tri_base += totals[1];
+        F = totals[0];
+        if (level_base + F > cap_nodes) return set_error(CRT_ERR_LIMIT, "GPU BVH node count overflow");
+        std::swap(cur, nxt);
+    }
+    uint32_t errbits = 0;
+    CRT_CUDA(cudaMemcpyAsync(&errbits, err, 4, cudaMemcpyDeviceToHost, s));
+    CRT_CUDA(cudaStreamSynchronize(s));
+    if (errbits) return set_error(CRT_ERR_CUDA, "GPU BVH build: inconsistent tree (" + std::to_string(errbits) + ")");
+    if (tri_base != n) return set_error(CRT_ERR_CUDA, "GPU BVH lost triangles");
+    *num_nodes = level_base;
+    *max_depth = depth;
+    *fnodes_ok = level_base <= (1u << 24);
+    return CRT_OK;
+}
+
+}  // namespace crt

@@ -52,6 +52,8 @@ struct crt_scene_s {
     bool default_f32 = false;       // encoding renders use unless told otherwise
     uint32_t n_mats = 0;
     bool ka_scaled = false;         // materials were given with the emission scaling applied
+    uint32_t builder = 0;           // crt_bvh_builder
+    bool host_bvh = true;           // `bvh` holds the device BVH (the GPU build fills it on demand)
     uint32_t generation = 0;        // bumped whenever the BVH buffers are replaced
     crt_scene_info info{};
 
@@ -86,6 +88,9 @@ struct WaveSet {
 };
 
 namespace crt {
+int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint32_t n, uint32_t max_levels,
+                  int max_children, DevBuf& nodes_out, DevBuf& fnodes_out, DevBuf& tris_out, uint32_t* num_nodes,
+                  uint32_t* max_depth, bool* fnodes_ok, cudaStream_t s);
 void destroy_wave_sets(struct ::crt_render_s* r);
 void drop_wave_graphs(struct ::crt_render_s* r);
 }

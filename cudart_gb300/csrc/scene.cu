@@ -66,6 +66,67 @@ static int install_bvh(crt_scene s, Bvh8& b, uint32_t width) {
     return CRT_OK;
 }
 
+// The GPU build leaves the BVH on the device only; export and rebuilds copy
+// it back on demand.
+static int ensure_host_bvh(crt_scene s) {
+    if (s->host_bvh) return CRT_OK;
+    Bvh8& b = s->bvh;
+    b.nodes.resize(s->info.num_nodes);
+    b.tris.resize(s->info.num_triangles);
+    b.fnodes.resize(b.fnodes_ok ? s->info.num_nodes : 0);
+    CRT_CUDA(cudaMemcpy(b.nodes.data(), s->nodes.p, b.nodes.size() * sizeof(Bvh8Node), cudaMemcpyDeviceToHost));
+    CRT_CUDA(cudaMemcpy(b.tris.data(), s->tris.p, b.tris.size() * sizeof(TriRecord), cudaMemcpyDeviceToHost));
+    if (b.fnodes_ok)
+        CRT_CUDA(cudaMemcpy(b.fnodes.data(), s->fnodes.p, b.fnodes.size() * sizeof(Bvh8FloatNode),
+                            cudaMemcpyDeviceToHost));
+    s->host_bvh = true;
+    return CRT_OK;
+}
+
+// Builds the BVH of v1/e1/e2 ([n][3]) with the scene's builder and installs it.
+static int build_and_install(crt_scene s, const std::vector<float>& v1, const std::vector<float>& e1,
+                             const std::vector<float>& e2, uint32_t n, uint32_t width) {
+    if (s->builder == CRT_BVH_GPU) {
+        DevBuf dv1, de1, de2, nodes, fnodes, tris;
+        int st = CRT_OK;
+        if ((st = upload(dv1, v1)) || (st = upload(de1, e1)) || (st = upload(de2, e2))) return st;
+        uint32_t nn = 0, depth = 0;
+        bool fok = false;
+        if ((st = build_bvh_gpu(dv1.as<float>(), de1.as<float>(), de2.as<float>(), n, (uint32_t)kMaxLevels,
+                                (int)width, nodes, fnodes, tris, &nn, &depth, &fok, nullptr)))
+            return st;
+        if (s->default_f32 && !fok)
+            return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
+        CRT_CUDA(cudaDeviceSynchronize());
+        s->nodes.swap(nodes);
+        s->fnodes.swap(fnodes);
+        s->tris.swap(tris);
+        s->bvh = Bvh8{};
+        s->bvh.fnodes_ok = fok;
+        s->bvh.max_depth = depth;
+        s->host_bvh = false;
+        s->dev.nodes = s->nodes.as<float4>();
+        s->dev.fnodes = fok ? s->fnodes.as<float4>() : nullptr;
+        s->dev.tris = s->tris.as<float4>();
+        crt_scene_info& I = s->info;
+        I.num_nodes = nn;
+        I.max_depth = depth;
+        I.node_bytes = (size_t)nn * (s->default_f32 ? sizeof(Bvh8FloatNode) : sizeof(Bvh8Node));
+        I.triangle_bytes = (size_t)n * sizeof(TriRecord);
+        I.bvh_width = width;
+        ++s->generation;
+        return CRT_OK;
+    }
+    Bvh8 bvh;
+    const char* msg = nullptr;
+    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, bvh, &msg, (int)width))
+        return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
+    if (s->default_f32 && !bvh.fnodes_ok)
+        return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
+    s->host_bvh = true;
+    return install_bvh(s, bvh, width);
+}
+
 inline float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
 inline float bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline float bits(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
@@ -149,6 +210,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     if (d->node_format > CRT_NODES_F32) return set_error(CRT_ERR_INVALID, "unknown node format");
     if (d->flags & ~(uint32_t)(CRT_SCENE_EDGES | CRT_SCENE_KA_SCALED))
         return set_error(CRT_ERR_INVALID, "unknown scene flag");
+    if (d->builder > CRT_BVH_GPU) return set_error(CRT_ERR_INVALID, "unknown BVH builder");
     if (d->bvh_width != 0 && d->bvh_width != 4 && d->bvh_width != 8)
         return set_error(CRT_ERR_INVALID, "bvh_width must be 4 or 8");
 
@@ -191,13 +253,8 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     cudaError_t dev_err = cudaGetDevice(&s->device);
     if (dev_err != cudaSuccess) { delete s; return cuda_error(dev_err, "cudaGetDevice"); }
 
-    const char* msg = nullptr;
     const uint32_t width = d->bvh_width ? d->bvh_width : 8u;
-    Bvh8 bvh;
-    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, bvh, &msg, (int)width)) {
-        delete s;
-        return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
-    }
+    s->builder = d->builder;
 
     // Per-face shading records.
     std::vector<float4> shade(3ull * n), uvs(2ull * n);
@@ -245,16 +302,12 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
     int st = CRT_OK;
     const bool f32 = d->node_format == CRT_NODES_F32;
-    if (f32 && !bvh.fnodes_ok) {
-        delete s;
-        return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
-    }
     // Both encodings go to the device (the FP32 one only while child indices
     // fit 24 bits); each render picks one.
     s->default_f32 = f32;
     s->n_mats = d->num_materials;
     s->ka_scaled = (d->flags & CRT_SCENE_KA_SCALED) != 0;
-    if ((st = install_bvh(s, bvh, width)) ||
+    if ((st = build_and_install(s, v1, e1, e2, n, width)) ||
         (st = upload(s->shade, shade)) || (st = upload(s->uvs, uvs)) || (st = upload(s->mats, mats)) ||
         (st = upload(s->light_geo, lgeo)) || (st = upload(s->texels, texels)) ||
         (st = upload(s->tex_dims, dims)) || (st = upload(s->tex_offsets, offs))) {
@@ -319,6 +372,8 @@ int crt_scene_set_bvh_width(crt_scene s, uint32_t width) {
     if (width != 4 && width != 8) return set_error(CRT_ERR_INVALID, "bvh_width must be 4 or 8");
     if (width == s->info.bvh_width) return CRT_OK;
     const auto t0 = std::chrono::steady_clock::now();
+    CRT_CUDA(cudaSetDevice(s->device));
+    if (int st = ensure_host_bvh(s)) return st;
     // the triangle records hold each face's v1, e1, e2 exactly as built
     const uint32_t n = s->info.num_triangles;
     std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n);
@@ -330,15 +385,8 @@ int crt_scene_set_bvh_width(crt_scene s, uint32_t width) {
             e2[3ull * f + k] = r.e2[k];
         }
     }
-    Bvh8 bvh;
-    const char* msg = nullptr;
-    if (!build_bvh8(v1.data(), e1.data(), e2.data(), n, (uint32_t)kMaxLevels, bvh, &msg, (int)width))
-        return set_error(CRT_ERR_LIMIT, msg ? msg : "BVH build failed");
-    if (s->default_f32 && !bvh.fnodes_ok)
-        return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; rebuilt BVH has more than 2^24 nodes");
-    CRT_CUDA(cudaSetDevice(s->device));
     CRT_CUDA(cudaDeviceSynchronize());   // nothing may still read the old nodes
-    int st = install_bvh(s, bvh, width);
+    int st = build_and_install(s, v1, e1, e2, n, width);
     if (st != CRT_OK) return st;
     s->info.build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return CRT_OK;
@@ -352,6 +400,8 @@ int crt_scene_get_info(crt_scene s, crt_scene_info* out) {
 
 int crt_scene_export_bvh(crt_scene s, void* nodes, void* triangles) {
     if (!s) return set_error(CRT_ERR_INVALID, "crt_scene_export_bvh: null scene");
+    CRT_CUDA(cudaSetDevice(s->device));
+    if (int st = ensure_host_bvh(s)) return st;
     if (nodes) std::memcpy(nodes, s->bvh.nodes.data(), s->bvh.nodes.size() * sizeof(Bvh8Node));
     if (triangles) std::memcpy(triangles, s->bvh.tris.data(), s->bvh.tris.size() * sizeof(TriRecord));
     return CRT_OK;

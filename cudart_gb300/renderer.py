@@ -85,7 +85,8 @@ class GB300Scene:
     """Scene handle: BVH, triangles, materials, lights and textures on the GPU."""
 
     def __init__(self, sc: SceneArrays, lights: Optional[np.ndarray] = None,
-                 node_format: str = "q8", bvh_width: int = 8, reference_layout: bool = False):
+                 node_format: str = "q8", bvh_width: int = 8, reference_layout: bool = False,
+                 builder: str = "host"):
         """reference_layout: pass the arrays the way the reference's Scene
         holds them after construction (CRT_SCENE_EDGES | CRT_SCENE_KA_SCALED:
         v1/e1/e2 per face, emission already multiplied by 3 x light area),
@@ -124,7 +125,8 @@ class GB300Scene:
                          len(lights) if lights is not None else 0,
                          li.ctypes.data if lights is not None else None,
                          len(sc.textures), dims.ctypes.data if len(dims) else None,
-                         texels.ctypes.data, NODE_FORMATS[node_format], bvh_width, flags)
+                         texels.ctypes.data, NODE_FORMATS[node_format], bvh_width, flags,
+                         {"host": _lib.BVH_HOST, "gpu": _lib.BVH_GPU}[builder])
         self.node_format = node_format
         self.bvh_width = bvh_width
         h = C.c_void_p()

@@ -111,6 +111,7 @@ typedef struct {
                                       encodings are uploaded */
     uint32_t bvh_width;            /* children per node: 4 or 8 (0 = 8) */
     uint32_t flags;                /* crt_scene_flags */
+    uint32_t builder;              /* crt_bvh_builder */
 } crt_scene_desc;
 
 /* Inputs as the reference's Scene holds them after construction, so a
@@ -121,6 +122,17 @@ typedef enum {
     CRT_SCENE_KA_SCALED = 2u   /* material ka already includes the emission
                                   scaling Ka * 3 * lights area (scene.cpp:163,177) */
 } crt_scene_flags;
+
+/* Where the BVH is built.  Both produce the same node and triangle layouts,
+ * so every query gives the same result; the trees differ, and with them the
+ * nodes a ray visits. */
+typedef enum {
+    CRT_BVH_HOST = 0u,   /* binned SAH (32 bins; exact sweep below 33 triangles),
+                            host threads: the best trees */
+    CRT_BVH_GPU = 1u     /* linear BVH over 30-bit Morton codes (Karras 2012) on
+                            the device, then the same collapse and encoding:
+                            tens of milliseconds for millions of triangles */
+} crt_bvh_builder;
 
 /* BVH node encoding on the device (same tree either way). */
 typedef enum {

@@ -21,6 +21,11 @@ def _decode(node, slot):
 
 def _check(positions, width=8):
     nodes, tris, depth = bvh_build_host(positions, width)
+    return check_tree(positions, nodes, tris, depth, width)
+
+
+def check_tree(positions, nodes, tris, depth, width=8):
+    """Invariants every build must meet (also used for the GPU build)."""
     n = len(positions)
     assert depth <= MAX_LEVELS
     assert sorted(tris["face"].tolist()) == list(range(n))
