@@ -1,6 +1,6 @@
 // bvh_gpu.cu -- GPU build of the 8-wide (or 4-wide) quantised BVH.
 //
-// A linear BVH over 30-bit Morton codes of the triangle centroids (Karras,
+// A linear BVH over 63-bit Morton codes of the triangle centroids (Karras,
 // "Maximizing parallelism in the construction of BVHs, octrees, and k-d
 // trees", HPG 2012), subtree boxes bottom-up, then the host build's
 // collapse and encoding (bvh8.cpp) run level by level: each wide node opens
@@ -105,43 +105,47 @@ __global__ void k_tri_boxes(const float* __restrict__ v1, const float* __restric
     }
 }
 
-__device__ __forceinline__ uint32_t spread10(uint32_t x) {
-    x &= 0x3FFu;
-    x = (x | (x << 16)) & 0x030000FFu;
-    x = (x | (x << 8)) & 0x0300F00Fu;
-    x = (x | (x << 4)) & 0x030C30C3u;
-    x = (x | (x << 2)) & 0x09249249u;
+// Spreads the low 21 bits of x to every third bit of a 63-bit code.
+__device__ __forceinline__ uint64_t spread21(uint64_t x) {
+    x &= 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
     return x;
 }
 
+// 63-bit Morton codes (21 bits per axis) of the centroids.
 __global__ void k_morton(const float* __restrict__ cent, uint32_t n, const uint32_t* __restrict__ cbounds,
-                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+                         uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     float lo[3], sc[3];
+    const float top = (float)((1u << 21) - 1u);
     for (int k = 0; k < 3; ++k) {
         lo[k] = order_float(cbounds[k]);
         const float ext = order_float(cbounds[3 + k]) - lo[k];
-        sc[k] = ext > 0.f ? 1023.f / ext : 0.f;
+        sc[k] = ext > 0.f ? top / ext : 0.f;
     }
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        uint32_t q[3];
+        uint64_t q[3];
         for (int k = 0; k < 3; ++k) {
             const float f = (cent[3ull * t + k] - lo[k]) * sc[k];
-            q[k] = (uint32_t)fminf(fmaxf(f, 0.f), 1023.f);
+            q[k] = (uint64_t)fminf(fmaxf(f, 0.f), top);
         }
-        keys[t] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+        keys[t] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
         vals[t] = t;
     }
 }
 
 // Length of the common prefix of sorted keys a and b (index order breaks ties).
-__device__ __forceinline__ int delta(const uint32_t* keys, int n, int a, int b) {
+__device__ __forceinline__ int delta(const uint64_t* keys, int n, int a, int b) {
     if (b < 0 || b >= n) return -1;
-    const uint32_t ka = keys[a], kb = keys[b];
-    if (ka == kb) return 32 + __clz((uint32_t)(a ^ b));
-    return __clz(ka ^ kb);
+    const uint64_t ka = keys[a], kb = keys[b];
+    if (ka == kb) return 64 + __clz((uint32_t)(a ^ b));
+    return __clzll(ka ^ kb);
 }
 
-__global__ void k_karras(const uint32_t* __restrict__ keys, int n, GNode* __restrict__ nodes, uint32_t* err) {
+__global__ void k_karras(const uint64_t* __restrict__ keys, int n, GNode* __restrict__ nodes, uint32_t* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     const int d = delta(keys, n, i, i + 1) > delta(keys, n, i, i - 1) ? 1 : -1;
@@ -412,18 +416,18 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
     CRT_CUDA(cudaMemcpyAsync(cbounds.p, init, 24, cudaMemcpyHostToDevice, s));
     k_tri_boxes<<<std::min<uint32_t>(blocks(n), 4096), kBlock, 0, s>>>(d_v1, d_e1, d_e2, n, margin, tbox.as<GBox>(),
                                                                         cent.as<float>(), cbounds.as<uint32_t>());
-    CRT_CUDA(keys.alloc((size_t)n * 4));
+    CRT_CUDA(keys.alloc((size_t)n * 8));
     CRT_CUDA(vals.alloc((size_t)n * 4));
-    CRT_CUDA(keys2.alloc((size_t)n * 4));
+    CRT_CUDA(keys2.alloc((size_t)n * 8));
     CRT_CUDA(perm.alloc((size_t)n * 4));
     k_morton<<<std::min<uint32_t>(blocks(n), 4096), kBlock, 0, s>>>(cent.as<float>(), n, cbounds.as<uint32_t>(),
-                                                                     keys.as<uint32_t>(), vals.as<uint32_t>());
+                                                                     keys.as<uint64_t>(), vals.as<uint32_t>());
     size_t tmp_bytes = 0;
-    CRT_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint32_t>(), keys2.as<uint32_t>(),
-                                             vals.as<uint32_t>(), perm.as<uint32_t>(), (int)n, 0, 30, s));
+    CRT_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                             vals.as<uint32_t>(), perm.as<uint32_t>(), (int)n, 0, 63, s));
     CRT_CUDA(tmp.alloc(tmp_bytes));
-    CRT_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint32_t>(), keys2.as<uint32_t>(),
-                                             vals.as<uint32_t>(), perm.as<uint32_t>(), (int)n, 0, 30, s));
+    CRT_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.as<uint64_t>(), keys2.as<uint64_t>(),
+                                             vals.as<uint32_t>(), perm.as<uint32_t>(), (int)n, 0, 63, s));
     const int ni = (int)n;
     CRT_CUDA(gnodes.alloc((size_t)(2 * n - 1) * sizeof(GNode)));
     CRT_CUDA(cudaMemsetAsync(gnodes.p, 0xFF, gnodes.bytes, s));   // every parent / child index starts at -1
@@ -431,7 +435,7 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
     k_leaves<<<blocks(n), kBlock, 0, s>>>(tbox.as<GBox>(), perm.as<uint32_t>(), ni, gn);
     int32_t root = (int32_t)n - 1;   // a lone triangle is its own root
     if (n > 1) {
-        k_karras<<<blocks(n - 1), kBlock, 0, s>>>(keys2.as<uint32_t>(), ni, gn, err);
+        k_karras<<<blocks(n - 1), kBlock, 0, s>>>(keys2.as<uint64_t>(), ni, gn, err);
         const int32_t none = -1;
         CRT_CUDA(cudaMemcpyAsync(&gn[0].parent, &none, 4, cudaMemcpyHostToDevice, s));
         CRT_CUDA(flags.alloc((size_t)n * 4));
