@@ -2,8 +2,8 @@
 //
 // Replaces the reference's binary SAH build (src/geometry/bvh.cpp:65-323,
 // 32-byte LinearBVHNode, two 1-D textures on the GPU) with:
-//   1. a binned surface-area-heuristic binary build (leaves of <= 3
-//      triangles, the reference's maxTrisInNode, bvh.cpp:62);
+//   1. a binned surface-area-heuristic binary build (leaves of <= 2
+//      triangles; the reference's maxTrisInNode is 3, bvh.cpp:62);
 //   2. a greedy collapse to 8-wide nodes (open the child with the largest
 //      surface area until 8 children);
 //   3. child slots ordered by octant so that visiting slot k ^ octant(ray)

@@ -129,7 +129,7 @@ typedef enum {
 typedef enum {
     CRT_BVH_HOST = 0u,   /* binned SAH (32 bins; exact sweep below 33 triangles),
                             host threads: the best trees */
-    CRT_BVH_GPU = 1u     /* linear BVH over 30-bit Morton codes (Karras 2012) on
+    CRT_BVH_GPU = 1u     /* linear BVH over 63-bit Morton codes (Karras 2012) on
                             the device, then the same collapse and encoding:
                             tens of milliseconds for millions of triangles */
 } crt_bvh_builder;
