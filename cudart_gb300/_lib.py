@@ -98,6 +98,16 @@ class TuneResult(C.Structure):
                 ("ms_per_spp", C.c_float), ("start_ms_per_spp", C.c_float), ("tune_ms", C.c_float)]
 
 
+class SceneFilesInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("num_meshes", C.c_uint32),
+                ("num_materials", C.c_uint32), ("num_mtl_materials", C.c_uint32),
+                ("num_textures", C.c_uint32), ("num_positions", C.c_uint32),
+                ("num_texcoords", C.c_uint32), ("num_normals", C.c_uint32),
+                ("num_polygons", C.c_uint32), ("file_bytes", C.c_uint64),
+                ("parse_ms", C.c_float), ("texture_ms", C.c_float)]
+
+
+LOAD_EXACT_MATERIALS = 1
 ADJOINT_EXACT_ROULETTE = 1
 BVH_HOST = 0
 BVH_GPU = 1
@@ -150,6 +160,14 @@ SIGNATURES = {
     "crt_render_view_info": (C.c_int, [P, U32, P, P, P]),
     "crt_render_view_resolve": (C.c_int, [P, U32, P]),
     "crt_render_view_accum": (C.c_int, [P, U32, P]),
+    "crt_scene_files_load": (C.c_int, [C.c_char_p, C.c_char_p, U32, P]),
+    "crt_scene_files_desc": (C.c_int, [P, P]),
+    "crt_scene_files_get_info": (C.c_int, [P, P]),
+    "crt_scene_files_mesh": (C.c_int, [P, U32, P, P, P]),
+    "crt_scene_files_destroy": (C.c_int, [P]),
+    "crt_camera_load_json": (C.c_int, [C.c_char_p, U32, U32, P]),
+    "crt_texture_load_png": (C.c_int, [C.c_char_p, P, P, U64]),
+    "crt_image_write_png": (C.c_int, [C.c_char_p, U32, U32, P]),
 }
 
 NOALLOC_MAX_PATHS = 65536

@@ -25,7 +25,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["scene.cu", "trace.cu", "render.cu", "wavefront.cu", "tune.cu", "bvh_gpu.cu"]
-CPP_SOURCES = ["bvh8.cpp"]
+CPP_SOURCES = ["bvh8.cpp", "ingest.cpp"]
 
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
                      "-prec-sqrt=true", "--expt-relaxed-constexpr",

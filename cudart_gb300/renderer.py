@@ -84,15 +84,32 @@ def _material_table(materials, kd=None, ka=None):
 class GB300Scene:
     """Scene handle: BVH, triangles, materials, lights and textures on the GPU."""
 
-    def __init__(self, sc: SceneArrays, lights: Optional[np.ndarray] = None,
+    def __init__(self, sc, lights: Optional[np.ndarray] = None,
                  node_format: str = "q8", bvh_width: int = 8, reference_layout: bool = False,
                  builder: str = "host"):
-        """reference_layout: pass the arrays the way the reference's Scene
+        """sc: SceneArrays, or ingest.SceneFiles (a scene read from OBJ/MTL/PNG
+        files by the library's loader).
+
+        reference_layout: pass the arrays the way the reference's Scene
         holds them after construction (CRT_SCENE_EDGES | CRT_SCENE_KA_SCALED:
         v1/e1/e2 per face, emission already multiplied by 3 x light area),
         which is what the C++ Renderer shim sends."""
         L = load()
         self.arrays = sc
+        self.node_format = node_format
+        self.bvh_width = bvh_width
+        builder_id = {"host": _lib.BVH_HOST, "gpu": _lib.BVH_GPU}[builder]
+        from .ingest import SceneFiles
+        if isinstance(sc, SceneFiles):
+            # straight from the loader's buffers (face-order emissive lights)
+            if reference_layout or lights is not None:
+                raise ValueError("a SceneFiles scene takes neither lights nor reference_layout")
+            desc = sc.desc()
+            desc.node_format, desc.bvh_width, desc.builder = NODE_FORMATS[node_format], bvh_width, builder_id
+            h = C.c_void_p()
+            check(L.crt_scene_create(C.byref(desc), C.byref(h)))
+            self.handle = h
+            return
         self._keep = []
         pos = np.ascontiguousarray(sc.positions, np.float32)
         nor = np.ascontiguousarray(sc.normals, np.float32)
@@ -126,9 +143,7 @@ class GB300Scene:
                          li.ctypes.data if lights is not None else None,
                          len(sc.textures), dims.ctypes.data if len(dims) else None,
                          texels.ctypes.data, NODE_FORMATS[node_format], bvh_width, flags,
-                         {"host": _lib.BVH_HOST, "gpu": _lib.BVH_GPU}[builder])
-        self.node_format = node_format
-        self.bvh_width = bvh_width
+                         builder_id)
         h = C.c_void_p()
         check(L.crt_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h

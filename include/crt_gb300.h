@@ -469,6 +469,69 @@ CRT_EXPORT int crt_autotune(crt_scene scene, const crt_camera* camera, uint32_t 
                             const crt_render_options* start, const crt_tune_params* params,
                             crt_tune_result* out);
 
+/* ---- scene files ----------------------------------------------------------
+ * The reference's input files read without its loaders, into the arrays
+ * crt_scene_desc takes (host memory owned by the handle):
+ *  - Wavefront OBJ with its `mtllib` libraries: objl::Loader::LoadFile /
+ *    LoadMaterials (src/include/obj_load.h:441-720, :1022-1170) as
+ *    Scene::loadObj + loadTriangles assemble them (src/geometry/scene.cpp:
+ *    40-46, 74-138): one record per face in file order; faces without
+ *    normals get (p0 - p1) x (p2 - p1) at every vertex; `usemtl` names map
+ *    to meshes by position as LoadFile maps them;
+ *  - the material table of populateMaterialsMap + materialFromMtl
+ *    (scene.cpp:175-203), including the reference's merging of materials
+ *    (unless CRT_LOAD_EXACT_MATERIALS); ka is the MTL Ka, scaled by
+ *    crt_scene_create as the reference scales it;
+ *  - PNG textures named by `map_Kd` (Scene::loadTextures, scene.cpp:55-71;
+ *    TextureStore::load, texture_store.cpp:18-35): linear texels
+ *    (float)pow(b / 255, 2.2) as stbi_loadf returns them.
+ * Departures, each for files the reference misreads or rejects: polygons
+ * are fanned into triangles; grey images give grey texels; runs of blanks
+ * separate tokens; a missing library, texture or malformed number is an
+ * error (CRT_ERR_INVALID with file:line in crt_last_error()).  The light
+ * list is left to crt_scene_create (emissive faces in face order). */
+typedef struct crt_scene_files_s* crt_scene_files;
+
+typedef enum {
+    CRT_LOAD_EXACT_MATERIALS = 1u   /* one table entry per MTL material in use
+                                       instead of the reference's merged table */
+} crt_load_flags;
+
+typedef struct {
+    uint32_t num_triangles;
+    uint32_t num_meshes;         /* meshes as LoadFile splits them (o, g, usemtl) */
+    uint32_t num_materials;      /* entries of the material table */
+    uint32_t num_mtl_materials;  /* materials read from the libraries */
+    uint32_t num_textures;
+    uint32_t num_positions;      /* v records */
+    uint32_t num_texcoords;      /* vt records */
+    uint32_t num_normals;        /* vn records */
+    uint32_t num_polygons;       /* faces of more than 3 vertices (fanned) */
+    uint64_t file_bytes;         /* OBJ + MTL + PNG bytes read */
+    float parse_ms;              /* OBJ + MTL */
+    float texture_ms;            /* PNG decode */
+} crt_scene_files_info;
+
+/* texture_dir is prefixed to each map_Kd name (a '/' is added if missing). */
+CRT_EXPORT int crt_scene_files_load(const char* obj_path, const char* texture_dir, uint32_t flags,
+                                    crt_scene_files* out);
+/* Fills desc with pointers into the handle (valid until it is destroyed);
+ * node_format, bvh_width, flags and builder are zero. */
+CRT_EXPORT int crt_scene_files_desc(crt_scene_files files, crt_scene_desc* desc);
+CRT_EXPORT int crt_scene_files_get_info(crt_scene_files files, crt_scene_files_info* out);
+CRT_EXPORT int crt_scene_files_mesh(crt_scene_files files, uint32_t mesh, const char** name,
+                                    uint32_t* first_triangle, uint32_t* num_triangles);
+CRT_EXPORT int crt_scene_files_destroy(crt_scene_files files);
+/* CameraJsonLoader (src/context/json_loader.cpp:15-48): keys fieldOfView,
+ * focalLength, fStop, eye, viewDirection, upDirection. */
+CRT_EXPORT int crt_camera_load_json(const char* path, uint32_t width, uint32_t height, crt_camera* out);
+/* One PNG as stbi_loadf + TextureStore::load read it: dims = {width,
+ * height}; with texels != NULL (capacity in texels) writes [w*h][rgb]. */
+CRT_EXPORT int crt_texture_load_png(const char* path, uint32_t dims[2], float* texels, uint64_t capacity);
+/* RGBA8 image to a PNG file (Launcher::saveToImage, src/context/
+ * launcher.cpp:13-21). */
+CRT_EXPORT int crt_image_write_png(const char* path, uint32_t width, uint32_t height, const uint8_t* rgba);
+
 #ifdef __cplusplus
 }
 #endif
