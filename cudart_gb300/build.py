@@ -51,6 +51,20 @@ def _stale(obj, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+CLI_SRC = os.path.join(HERE, "cli", "crt_render.cpp")
+CLI = os.path.join(HERE, "crt_render")
+
+
+def _build_cli(cxx: str, verbose: bool) -> None:
+    """The command-line renderer, linked against the in-tree library."""
+    if not _stale(CLI, [CLI_SRC, LIB, os.path.join(HERE, "..", "include", "crt_gb300.h")]):
+        return
+    tmp = CLI + ".tmp"
+    _run([cxx, "-O2", "-std=c++17", CLI_SRC, "-o", tmp, "-L" + HERE, "-lcrt_gb300",
+          "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath-link,{CUDA_HOME}/lib64"], verbose)
+    os.replace(tmp, CLI)
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     """Compile every CUDA/C++ source of the library and link the .so."""
     os.makedirs(OUT_DIR, exist_ok=True)
@@ -78,6 +92,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", tmp] + objs +
              ["-Xlinker", f"-rpath,{CUDA_HOME}/lib64", "-lpthread"], verbose)
         os.replace(tmp, LIB)
+    _build_cli(cxx, verbose)
     if ptxas_info:
         print("\n".join(outputs))
     return LIB

@@ -20,6 +20,11 @@
 #include <atomic>
 #include <charconv>
 #include <chrono>
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -36,8 +41,23 @@ namespace crt {
 int set_error(int status, const std::string& msg);
 }
 
+// Per-face arrays written once, in parallel, by the face pass: left
+// uninitialised until then (no serial zero fill).
+template <class T>
+struct RawArray {
+    std::unique_ptr<T[]> p;
+    size_t n = 0;
+    void allocate(size_t count) {
+        p.reset(new T[count]);
+        n = count;
+    }
+    T* data() { return p.get(); }
+    const T* data() const { return p.get(); }
+    T& operator[](size_t i) { return p[i]; }
+};
+
 struct crt_scene_files_s {
-    std::vector<float> positions, normals, uvs;   // [n][3][3], [n][3][3], [n][3][2]
+    RawArray<float> positions, normals, uvs;      // [n][3][3], [n][3][3], [n][3][2]
     std::vector<uint32_t> material_ids;
     std::vector<crt_material> materials;
     std::vector<uint32_t> texture_dims;
@@ -96,6 +116,48 @@ bool read_file(const std::string& path, std::string& out, std::string& err) {
         err = "short read of " + path;
         return false;
     }
+    return true;
+}
+
+// Read-only view of a whole file: a private memory map, so that the parse
+// threads fault the pages in parallel instead of one thread copying them.
+struct FileView {
+    const char* data = "";
+    size_t size = 0;
+    void* map = nullptr;
+    FileView() = default;
+    FileView(const FileView&) = delete;
+    FileView& operator=(const FileView&) = delete;
+    ~FileView() {
+        if (map) munmap(map, size);
+    }
+};
+
+bool map_file(const std::string& path, FileView& fv, std::string& err) {
+    const int fd = open(path.c_str(), O_RDONLY);
+    if (fd < 0) {
+        err = "cannot open " + path;
+        return false;
+    }
+    struct stat st;
+    if (fstat(fd, &st) != 0 || !S_ISREG(st.st_mode)) {
+        close(fd);
+        err = "cannot read " + path;
+        return false;
+    }
+    fv.size = (size_t)st.st_size;
+    if (fv.size) {
+        void* m = mmap(nullptr, fv.size, PROT_READ, MAP_PRIVATE, fd, 0);
+        if (m == MAP_FAILED) {
+            close(fd);
+            err = "cannot map " + path;
+            return false;
+        }
+        madvise(m, fv.size, MADV_WILLNEED);
+        fv.map = m;
+        fv.data = static_cast<const char*>(m);
+    }
+    close(fd);
     return true;
 }
 
@@ -170,7 +232,7 @@ bool parse_int(std::string_view tok, long long& out) {
 }
 
 // ---------------------------------------------------------------------------
-// MTL (objl::Loader::LoadMaterials, src/include/obj_load.h:1022-1170 with
+// MTL (objl::Loader::LoadMaterials, src/include/obj_load.h:1015-1186 with
 // CudaRT's `type` and `diffuse` keys; defaults of objl::Material,
 // obj_load.h:151-161: Ni = 0, type LAMBERT)
 // ---------------------------------------------------------------------------
@@ -322,7 +384,7 @@ crt_material to_abi(const TableMaterial& t) {
 
 // ---------------------------------------------------------------------------
 // OBJ (objl::Loader::LoadFile, obj_load.h:441-720; faces as
-// GenVerticesFromRawOBJ, :730-833)
+// GenVerticesFromRawOBJ, :730-844)
 // ---------------------------------------------------------------------------
 enum LineKind : uint8_t { L_OTHER, L_V, L_VT, L_VN, L_F, L_GROUP, L_USEMTL, L_MTLLIB };
 
@@ -1154,21 +1216,22 @@ int load_scene_files(const std::string& obj_path, const std::string& texture_dir
                      crt_scene_files_s& S) {
     const auto t0 = Clock::now();
     if (!ends_with(obj_path, ".obj")) return set_error(CRT_ERR_INVALID, "scene file is not a .obj file: " + obj_path);
-    std::string text, err;
-    if (!read_file(obj_path, text, err)) return set_error(CRT_ERR_INVALID, err);
-    S.info.file_bytes = text.size();
-    const char* base = text.data();
-    const char* end = base + text.size();
+    FileView text;
+    std::string err;
+    if (!map_file(obj_path, text, err)) return set_error(CRT_ERR_INVALID, err);
+    S.info.file_bytes = text.size;
+    const char* base = text.data;
+    const char* end = base + text.size;
 
     // line-aligned chunks of ~4 MB (at least one per thread for large files)
     const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t want = std::max<size_t>(1, std::min(text.size() / (1u << 16) + 1,
-                                                     std::max(hw * 4, text.size() / (4u << 20) + 1)));
+    const size_t want = std::max<size_t>(1, std::min(text.size / (1u << 16) + 1,
+                                                     std::max(hw * 4, text.size / (4u << 20) + 1)));
     std::vector<Chunk> chunks;
     {
         const char* p = base;
         for (size_t k = 0; k < want && p < end; ++k) {
-            const char* q = k + 1 == want ? end : base + (text.size() * (k + 1)) / want;
+            const char* q = k + 1 == want ? end : base + (text.size * (k + 1)) / want;
             if (q < p) q = p;
             if (q < end) {
                 const char* nl = static_cast<const char*>(std::memchr(q, '\n', (size_t)(end - q)));
@@ -1240,7 +1303,10 @@ int load_scene_files(const std::string& obj_path, const std::string& texture_dir
     if (ntri >= (1ull << 31)) return set_error(CRT_ERR_LIMIT, obj_path + ": more than 2^31 triangles");
 
     // pass 2: v / vt / vn records
-    std::vector<float> P(3 * nv), T(2 * nvt), N(3 * nvn);
+    RawArray<float> P, T, N;
+    P.allocate(3 * nv);
+    T.allocate(2 * nvt);
+    N.allocate(3 * nvn);
     parallel_for(chunks.size(), [&](size_t ci) {
         Chunk& C = chunks[ci];
         uint64_t iv = C.v0, ivt = C.vt0, ivn = C.vn0, line = 0;
@@ -1274,9 +1340,9 @@ int load_scene_files(const std::string& obj_path, const std::string& texture_dir
     if (int st = first_error()) return st;
 
     // pass 3: faces, fanned into triangles (0, j, j + 1)
-    S.positions.assign(9 * ntri, 0.f);
-    S.normals.assign(9 * ntri, 0.f);
-    S.uvs.assign(6 * ntri, 0.f);
+    S.positions.allocate(9 * ntri);
+    S.normals.allocate(9 * ntri);
+    S.uvs.allocate(6 * ntri);
     parallel_for(chunks.size(), [&](size_t ci) {
         Chunk& C = chunks[ci];
         uint64_t cv = C.v0, cvt = C.vt0, cvn = C.vn0, tri = C.tri0, line = 0;
@@ -1318,7 +1384,7 @@ int load_scene_files(const std::string& obj_path, const std::string& texture_dir
             }
             if (!all_normals) {
                 // a face with any vertex lacking a normal gets the unnormalised
-                // (p0 - p1) x (p2 - p1) on every vertex (obj_load.h:820-832)
+                // (p0 - p1) x (p2 - p1) on every vertex (obj_load.h:832-843)
                 const float A[3] = {vp[0] - vp[3], vp[1] - vp[4], vp[2] - vp[5]};
                 const float B[3] = {vp[6] - vp[3], vp[7] - vp[4], vp[8] - vp[5]};
                 const float c[3] = {A[1] * B[2] - A[2] * B[1], A[2] * B[0] - A[0] * B[2],

@@ -473,7 +473,7 @@ CRT_EXPORT int crt_autotune(crt_scene scene, const crt_camera* camera, uint32_t 
  * The reference's input files read without its loaders, into the arrays
  * crt_scene_desc takes (host memory owned by the handle):
  *  - Wavefront OBJ with its `mtllib` libraries: objl::Loader::LoadFile /
- *    LoadMaterials (src/include/obj_load.h:441-720, :1022-1170) as
+ *    LoadMaterials (src/include/obj_load.h:441-720, :1015-1186) as
  *    Scene::loadObj + loadTriangles assemble them (src/geometry/scene.cpp:
  *    40-46, 74-138): one record per face in file order; faces without
  *    normals get (p0 - p1) x (p2 - p1) at every vertex; `usemtl` names map

@@ -22,6 +22,7 @@
 #include "scene.h"
 
 #include <cfloat>
+#include <chrono>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -319,6 +320,27 @@ __attribute__((visibility("default"))) void ref_render(const uint32_t* pixels, u
         }
         acc[3 * k] = a.x; acc[3 * k + 1] = a.y; acc[3 * k + 2] = a.z;
         for (int ch = 0; ch < 3; ++ch) { mean[3 * k + ch] = mu[ch]; m2[3 * k + ch] = q[ch]; }
+    }
+}
+
+/* Wall time of the reference's file loading alone (main.cpp:133-137 up to
+ * loadTriangles: OBJ + MTL, camera JSON, textures, triangle assembly), in
+ * milliseconds; -1 on an exception.  Leaves the scene half built: call it
+ * in a process of its own. */
+__attribute__((visibility("default"))) double ref_time_load(const char* obj, const char* cam,
+                                                            const char* tex_dir, int width,
+                                                            int height) {
+    try {
+        auto t0 = std::chrono::steady_clock::now();
+        Scene* s = new Scene();
+        s->loadObj(obj);
+        s->loadCamera(cam, (pixels_t)width, (pixels_t)height);
+        s->loadTextures(tex_dir);
+        s->loadTriangles();
+        auto t1 = std::chrono::steady_clock::now();
+        return std::chrono::duration<double, std::milli>(t1 - t0).count();
+    } catch (const std::exception&) {
+        return -1.0;
     }
 }
 
