@@ -502,6 +502,30 @@ def run_gb300(args):
         print(json.dumps(out), flush=True)
 
 
+def run_build_only(args) -> None:
+    """Scene creation alone (host arrays -> device scene with its BVH), the
+    part of the end-to-end step before rendering; one JSON line."""
+    import torch
+    from cudart_gb300 import GB300Scene, scenes
+    sc = scenes.large_textured() if not args.small else scenes.large_textured(
+        width=480, height=270, grid=256, tex_size=256)
+    wall, build = [], []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s = GB300Scene(sc, builder=args.build_only)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            wall.append(time.perf_counter() - t0)
+            build.append(s.info.build_ms)
+        info = s.info
+        del s
+    print(json.dumps({"metric": "scene_create_ms", "builder": args.build_only, "triangles": sc.n_tris,
+                      "nodes": int(info.num_nodes), "max_depth": int(info.max_depth),
+                      "wall_ms": round(1e3 * statistics.median(wall), 2),
+                      "build_ms": round(statistics.median(build), 2), "steps": args.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -516,8 +540,12 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the batched-views and adjoint legs")
     ap.add_argument("--c4-spp-div", type=int, default=4, help="batched views: spp divisor")
     ap.add_argument("--inversion-iters", type=int, default=200)
+    ap.add_argument("--build-only", choices=["gpu", "host"], default=None,
+                    help="time crt_scene_create with this BVH builder on the 1080p scene and exit")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.build_only:
+        run_build_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)
