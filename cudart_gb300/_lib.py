@@ -54,7 +54,7 @@ class SceneDesc(C.Structure):
                 ("num_lights", C.c_uint32), ("light_indices", C.c_void_p),
                 ("num_textures", C.c_uint32), ("texture_dims", C.c_void_p),
                 ("texels", C.c_void_p), ("node_format", C.c_uint32), ("bvh_width", C.c_uint32),
-                ("flags", C.c_uint32), ("builder", C.c_uint32)]
+                ("flags", C.c_uint32), ("builder", C.c_uint32), ("texels_rgba8", C.c_void_p)]
 
 
 NODES_Q8 = 0

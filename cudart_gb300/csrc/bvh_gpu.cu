@@ -1,15 +1,19 @@
 // bvh_gpu.cu -- GPU build of the 8-wide (or 4-wide) quantised BVH.
 //
-// A linear BVH over 63-bit Morton codes of the triangle centroids (Karras,
-// "Maximizing parallelism in the construction of BVHs, octrees, and k-d
-// trees", HPG 2012), subtree boxes bottom-up, then the host build's
-// collapse and encoding (bvh8.cpp) run level by level: each wide node opens
-// its largest-area internal children until it has 8 (or 4), assigns them to
-// slots by octant, and quantises their boxes outward on a power-of-two grid.
-// A subtree of at most 3 triangles becomes a leaf slot (the reference's leaf
-// size, bvh.cpp:62).  Node and triangle layouts are the host build's, so the
-// traversal kernels and every query result are unchanged; only the tree
-// differs, and with it the number of nodes a ray visits.
+// Binary hierarchy by parallel locally-ordered clustering (PLOC: Meister and
+// Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume
+// Hierarchy Construction", IEEE TVCG 2018): triangles sorted by 63-bit
+// Morton codes of their centroids start as clusters; every iteration each
+// cluster finds, among the clusters within kRadius places of it in Morton
+// order, the one whose merged box has the least surface area; mutual
+// nearest neighbours merge (the merged cluster keeps the left one's place),
+// and the list is compacted.  Then the host build's collapse and encoding
+// (bvh8.cpp) run level by level: each wide node opens its largest-area
+// internal children until it has 8 (or 4), assigns them to slots by octant,
+// and quantises their boxes outward on a power-of-two grid.  A subtree of at
+// most kLeafMaxGpu triangles becomes a leaf slot.  Node and triangle layouts
+// are the host build's, so the traversal kernels and every query result are
+// unchanged; only the tree differs, and with it the nodes a ray visits.
 //
 // Triangle boxes get the host build's conservative margin (2^-15 of the
 // largest coordinate magnitude, computed in FP64 and rounded outward).
@@ -17,6 +21,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <vector>
 
@@ -25,15 +30,23 @@
 namespace crt {
 namespace {
 
-constexpr uint32_t kLeafMaxGpu = 3;
+#ifndef CRT_GPU_LEAF_MAX
+#define CRT_GPU_LEAF_MAX 2             // as the host build's leaves
+#endif
+#ifndef CRT_PLOC_RADIUS
+#define CRT_PLOC_RADIUS 16             // PLOC search radius (clusters on each side)
+#endif
+constexpr uint32_t kLeafMaxGpu = CRT_GPU_LEAF_MAX;
 constexpr int kBlock = 256;
+constexpr int kRadius = CRT_PLOC_RADIUS;
 
 struct GBox {
     float lo[3], hi[3];
 };
 
-// Binary nodes: internal k at index k (0..n-2), triangle i (sorted order) at
-// n-1+i.  [first, first+count) is the node's range of sorted triangles.
+// Binary nodes: internal nodes at 0..n-2 (the root at 0, created last),
+// triangle i of the sorted order at n-1+i.  `count` is the node's number of
+// triangles; a leaf's `first` is its sorted position.
 struct GNode {
     GBox box;
     int32_t left, right, parent;
@@ -137,48 +150,6 @@ __global__ void k_morton(const float* __restrict__ cent, uint32_t n, const uint3
     }
 }
 
-// Length of the common prefix of sorted keys a and b (index order breaks ties).
-__device__ __forceinline__ int delta(const uint64_t* keys, int n, int a, int b) {
-    if (b < 0 || b >= n) return -1;
-    const uint64_t ka = keys[a], kb = keys[b];
-    if (ka == kb) return 64 + __clz((uint32_t)(a ^ b));
-    return __clzll(ka ^ kb);
-}
-
-__global__ void k_karras(const uint64_t* __restrict__ keys, int n, GNode* __restrict__ nodes, uint32_t* err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int d = delta(keys, n, i, i + 1) > delta(keys, n, i, i - 1) ? 1 : -1;
-    const int dmin = delta(keys, n, i, i - d);
-    int lmax = 2;
-    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
-    int l = 0;
-    for (int t = lmax / 2; t >= 1; t /= 2)
-        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = delta(keys, n, i, j);
-    int s = 0;
-    for (int t = (l + 1) / 2;; t = (t + 1) / 2) {
-        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
-        if (t == 1) break;
-    }
-    const int gamma = i + s * d + min(d, 0);
-    const int first = min(i, j), last = max(i, j);
-    const int left = (first == gamma) ? (n - 1 + gamma) : gamma;
-    const int right = (last == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
-    if (gamma < first || gamma + 1 > last || left <= 0 || right <= 0 || left > 2 * n - 2 || right > 2 * n - 2) {
-        atomicOr(err, 1u);   // never expected; keeps every write in bounds
-        return;
-    }
-    GNode& me = nodes[i];
-    me.left = left;
-    me.right = right;
-    me.first = (uint32_t)first;
-    me.count = (uint32_t)(last - first + 1);
-    nodes[left].parent = i;
-    nodes[right].parent = i;
-}
-
 __global__ void k_leaves(const GBox* __restrict__ tbox, const uint32_t* __restrict__ perm, int n,
                          GNode* __restrict__ nodes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -190,33 +161,106 @@ __global__ void k_leaves(const GBox* __restrict__ tbox, const uint32_t* __restri
     lf.count = 1;
 }
 
-// Boxes of the internal nodes: the second child to finish computes the parent.
-__global__ void k_bottom_up(int n, GNode* nodes, uint32_t* flags, uint32_t* err) {
+// PLOC nearest neighbour: for cluster i of m (in Morton order), the cluster
+// j within kRadius places whose merged box has the least half area.  Pairs
+// are ordered by (area, |i - j|, min(i, j) odd, min(i, j)): a total order on
+// unordered pairs, so the best pair overall is always mutual and every
+// iteration merges; among equal boxes (2k, 2k + 1) pair up, so even a scene
+// of identical triangles halves its clusters every iteration.
+__global__ void k_ploc_nn(const int32_t* __restrict__ clusters, int m, const GNode* __restrict__ nodes,
+                          int32_t* __restrict__ nn, int n, uint32_t* err) {
+    __shared__ GBox tile[kBlock + 2 * kRadius];
+    const int b0 = blockIdx.x * kBlock;
+    const int lo = max(0, b0 - kRadius), hi = min(m, b0 + kBlock + kRadius);   // [lo, hi) staged
+    for (int k = lo + (int)threadIdx.x; k < hi; k += kBlock) {
+        const int32_t c = clusters[k];
+        if (c < 0 || c > 2 * n - 2) {   // never expected; keeps the read in bounds
+            atomicOr(err, 1u);
+            tile[k - lo] = GBox{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        } else {
+            tile[k - lo] = nodes[c].box;
+        }
+    }
+    __syncthreads();
+    const int i = b0 + (int)threadIdx.x;
+    if (i >= m) return;
+    const GBox bi = tile[i - lo];
+    float best = FLT_MAX;
+    int bj = -1, bdist = INT_MAX, bodd = 1, bmin = INT_MAX;
+    const int j0 = max(0, i - kRadius), j1 = min(m - 1, i + kRadius);
+    for (int j = j0; j <= j1; ++j) {
+        if (j == i) continue;
+        GBox u = bi;
+        grow(u, tile[j - lo]);
+        const float d = half_area(u);
+        const int dist = abs(i - j), mn = min(i, j), odd = mn & 1;
+        const bool better =
+            d < best || (d == best && (dist < bdist || (dist == bdist && (odd < bodd || (odd == bodd && mn < bmin)))));
+        if (better) {
+            best = d;
+            bj = j;
+            bdist = dist;
+            bodd = odd;
+            bmin = mn;
+        }
+    }
+    nn[i] = bj;
+}
+
+// Merge flags, packed for one 64-bit scan: high word = cluster survives
+// (kept or merged into), low word = a new node is created here.
+__global__ void k_ploc_flags(const int32_t* __restrict__ nn, int m, uint64_t* __restrict__ flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int p = nodes[n - 1 + i].parent;
-    for (int climbed = 0; p >= 0; ++climbed) {
-        if (p > n - 2 || climbed >= n) {   // never expected; ends the climb
-            atomicOr(err, 8u);
+    if (i >= m) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && j < m && nn[j] == i;
+    const bool create = mutual && i < j;
+    const bool survive = !mutual || i < j;
+    flags[i] = ((uint64_t)survive << 32) | (uint64_t)create;
+}
+
+__global__ void k_ploc_init(int32_t* __restrict__ clusters, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) clusters[i] = n - 1 + i;   // every triangle is a cluster
+}
+
+// Creates the merged nodes (ids counting down from `next_id`) and writes the
+// compacted cluster list.
+__global__ void k_ploc_merge(const int32_t* __restrict__ clusters, const int32_t* __restrict__ nn, int m,
+                             const uint64_t* __restrict__ scan, int32_t next_id, GNode* __restrict__ nodes,
+                             int32_t* __restrict__ out, int n, uint32_t* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && j < m && nn[j] == i;
+    if (mutual && i > j) return;   // merged into cluster j
+    const uint64_t sc = scan[i];
+    const uint32_t pos = (uint32_t)(sc >> 32);
+    int32_t id = clusters[i];
+    if (mutual) {
+        id = next_id - (int32_t)(uint32_t)(sc & 0xFFFFFFFFull);
+        const int32_t l = clusters[i], r = clusters[j];
+        if (id < 0 || id > n - 2 || l < 0 || r < 0 || l > 2 * n - 2 || r > 2 * n - 2) {
+            atomicOr(err, 1u);   // never expected; keeps every write in bounds
             return;
         }
-        __threadfence();
-        if (atomicAdd(&flags[p], 1u) == 0) return;   // the sibling subtree is not done yet
-        __threadfence();
-        const int l = __ldcg(&nodes[p].left), r = __ldcg(&nodes[p].right);
-        GBox b;
-        for (int k = 0; k < 3; ++k) {
-            b.lo[k] = fminf(__ldcg(&nodes[l].box.lo[k]), __ldcg(&nodes[r].box.lo[k]));
-            b.hi[k] = fmaxf(__ldcg(&nodes[l].box.hi[k]), __ldcg(&nodes[r].box.hi[k]));
-        }
-        __stcg(&nodes[p].box.lo[0], b.lo[0]);
-        __stcg(&nodes[p].box.lo[1], b.lo[1]);
-        __stcg(&nodes[p].box.lo[2], b.lo[2]);
-        __stcg(&nodes[p].box.hi[0], b.hi[0]);
-        __stcg(&nodes[p].box.hi[1], b.hi[1]);
-        __stcg(&nodes[p].box.hi[2], b.hi[2]);
-        p = __ldcg(&nodes[p].parent);
+        GNode nd;
+        nd.box = nodes[l].box;
+        grow(nd.box, nodes[r].box);
+        nd.left = l;
+        nd.right = r;
+        nd.parent = -1;
+        nd.first = 0;
+        nd.count = nodes[l].count + nodes[r].count;
+        nodes[id] = nd;
+        nodes[l].parent = id;
+        nodes[r].parent = id;
     }
+    if (pos >= (uint32_t)m) {
+        atomicOr(err, 1u);
+        return;
+    }
+    out[pos] = id;
 }
 
 __device__ __forceinline__ bool opens(const GNode& nd) { return nd.count > kLeafMaxGpu; }
@@ -359,8 +403,30 @@ __global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t leve
             else atomicOr(err, 2u);
         } else {
             node.meta[s] = (uint8_t)((cn.count << 5) | tri_o);
-            for (uint32_t i = 0; i < cn.count; ++i) {
-                const uint32_t t = perm[cn.first + i];
+            // the subtree's triangles, left to right (at most kLeafMaxGpu)
+            uint32_t pos[kLeafMaxGpu];
+            uint32_t np = 0;
+            int32_t stack[2 * kLeafMaxGpu];
+            int sp = 0;
+            stack[sp++] = w.ch[c];
+            while (sp > 0) {
+                const int32_t x = stack[--sp];
+                if (x < 0 || x > 2 * (int32_t)n_tris - 2) { atomicOr(err, 4u); break; }
+                const GNode& g = nodes[x];
+                if (g.left < 0) {
+                    if (np < kLeafMaxGpu) pos[np++] = g.first;
+                    else atomicOr(err, 4u);
+                } else if (sp + 2 <= 2 * (int)kLeafMaxGpu) {
+                    stack[sp++] = g.right;
+                    stack[sp++] = g.left;
+                } else {
+                    atomicOr(err, 4u);
+                    break;
+                }
+            }
+            if (np != cn.count) atomicOr(err, 4u);
+            for (uint32_t i = 0; i < np; ++i) {
+                const uint32_t t = perm[pos[i]];
                 TriRecord r;
                 for (int k = 0; k < 3; ++k) {
                     r.v1[k] = v1[3ull * t + k];
@@ -372,7 +438,7 @@ __global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t leve
                 if (node.tri_base + tri_o + i < n_tris) tris[node.tri_base + tri_o + i] = r;
                 else atomicOr(err, 4u);
             }
-            tri_o += cn.count;
+            tri_o += np;
         }
     }
     out[level_base + f] = node;
@@ -394,7 +460,7 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
                   uint32_t* max_depth, bool* fnodes_ok, cudaStream_t s) {
     if (n == 0) return set_error(CRT_ERR_INVALID, "scene has no triangles");
     if (n >= (1u << 30)) return set_error(CRT_ERR_LIMIT, "GPU BVH build: at most 2^30 triangles");
-    DevBuf maxbits, tbox, cent, cbounds, keys, vals, keys2, perm, gnodes, flags, tmp, errbuf;
+    DevBuf maxbits, tbox, cent, cbounds, keys, vals, keys2, perm, gnodes, tmp, errbuf;
     CRT_CUDA(errbuf.alloc(4));
     CRT_CUDA(cudaMemsetAsync(errbuf.p, 0, 4, s));
     uint32_t* err = errbuf.as<uint32_t>();
@@ -435,16 +501,44 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
     k_leaves<<<blocks(n), kBlock, 0, s>>>(tbox.as<GBox>(), perm.as<uint32_t>(), ni, gn);
     int32_t root = (int32_t)n - 1;   // a lone triangle is its own root
     if (n > 1) {
-        k_karras<<<blocks(n - 1), kBlock, 0, s>>>(keys2.as<uint64_t>(), ni, gn, err);
-        const int32_t none = -1;
-        CRT_CUDA(cudaMemcpyAsync(&gn[0].parent, &none, 4, cudaMemcpyHostToDevice, s));
-        CRT_CUDA(flags.alloc((size_t)n * 4));
-        CRT_CUDA(cudaMemsetAsync(flags.p, 0, (size_t)n * 4, s));
-        k_bottom_up<<<blocks(n), kBlock, 0, s>>>(ni, gn, flags.as<uint32_t>(), err);
-        root = 0;
-    } else {
-        const int32_t none = -1;
-        CRT_CUDA(cudaMemcpyAsync(&gn[0].parent, &none, 4, cudaMemcpyHostToDevice, s));
+        // PLOC iterations over the cluster list (Morton order), ping-ponged
+        DevBuf cl_a, cl_b, nnb, fl, scan, ploc_tmp;
+        CRT_CUDA(cl_a.alloc((size_t)n * 4));
+        CRT_CUDA(cl_b.alloc((size_t)n * 4));
+        CRT_CUDA(nnb.alloc((size_t)n * 4));
+        CRT_CUDA(fl.alloc((size_t)(n + 1) * 8));
+        CRT_CUDA(scan.alloc((size_t)(n + 1) * 8));
+        k_ploc_init<<<blocks(n), kBlock, 0, s>>>(cl_a.as<int32_t>(), ni);
+        size_t ploc_bytes = 0;
+        CRT_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, ploc_bytes, fl.as<uint64_t>(), scan.as<uint64_t>(),
+                                               (int)n + 1, s));
+        CRT_CUDA(ploc_tmp.alloc(ploc_bytes));
+        int32_t* cur = cl_a.as<int32_t>();
+        int32_t* nxt = cl_b.as<int32_t>();
+        uint32_t m = n;
+        int32_t next_id = (int32_t)n - 2;
+        for (uint32_t iter = 0; m > 1; ++iter) {
+            if (iter >= n) return set_error(CRT_ERR_CUDA, "GPU BVH build: clustering did not converge");
+            k_ploc_nn<<<blocks(m), kBlock, 0, s>>>(cur, (int)m, gn, nnb.as<int32_t>(), ni, err);
+            k_ploc_flags<<<blocks(m), kBlock, 0, s>>>(nnb.as<int32_t>(), (int)m, fl.as<uint64_t>());
+            CRT_CUDA(cudaMemsetAsync(fl.as<uint64_t>() + m, 0, 8, s));
+            CRT_CUDA(cub::DeviceScan::ExclusiveSum(ploc_tmp.p, ploc_bytes, fl.as<uint64_t>(), scan.as<uint64_t>(),
+                                                   (int)m + 1, s));
+            k_ploc_merge<<<blocks(m), kBlock, 0, s>>>(cur, nnb.as<int32_t>(), (int)m, scan.as<uint64_t>(), next_id,
+                                                      gn, nxt, ni, err);
+            uint64_t total = 0;
+            CRT_CUDA(cudaMemcpyAsync(&total, scan.as<uint64_t>() + m, 8, cudaMemcpyDeviceToHost, s));
+            CRT_CUDA(cudaStreamSynchronize(s));
+            const uint32_t survivors = (uint32_t)(total >> 32), merges = (uint32_t)(total & 0xFFFFFFFFull);
+            if (merges == 0 || survivors + merges != m || (int64_t)next_id + 1 < (int64_t)merges)
+                return set_error(CRT_ERR_CUDA, "GPU BVH build: inconsistent clustering step");
+            m = survivors;
+            next_id -= (int32_t)merges;
+            std::swap(cur, nxt);
+        }
+        CRT_CUDA(cudaMemcpyAsync(&root, cur, 4, cudaMemcpyDeviceToHost, s));
+        CRT_CUDA(cudaStreamSynchronize(s));
+        if (root != 0 || next_id != -1) return set_error(CRT_ERR_CUDA, "GPU BVH build: clustering left no single root");
     }
     CRT_CUDA(cudaGetLastError());
     {   // the collapse follows child links: stop here if any were not set

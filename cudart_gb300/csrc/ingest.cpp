@@ -39,6 +39,7 @@
 
 namespace crt {
 int set_error(int status, const std::string& msg);
+const float* stb_texel_table();
 }
 
 // Per-face arrays written once, in parallel, by the face pass: left
@@ -729,6 +730,13 @@ const float* gamma_lut() {
     }();
     return lut.data();
 }
+
+}  // namespace
+
+// The same table for crt_scene_create's RGBA8 texels.
+const float* crt::stb_texel_table() { return gamma_lut(); }
+
+namespace {
 
 // Decodes a PNG file into rgb texels (8-bit sample values per channel).
 struct Png {

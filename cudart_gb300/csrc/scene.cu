@@ -13,6 +13,9 @@
 
 namespace crt {
 
+// stbi_loadf's 8-bit to float table (defined with the PNG reader).
+const float* stb_texel_table();
+
 namespace {
 thread_local std::string g_last_error;
 }
@@ -83,39 +86,46 @@ static int ensure_host_bvh(crt_scene s) {
     return CRT_OK;
 }
 
-// Builds the BVH of v1/e1/e2 ([n][3]) with the scene's builder and installs it.
+// Builds the BVH of device arrays v1/e1/e2 ([n][3]) on the GPU and installs it.
+static int build_on_device(crt_scene s, const float* dv1, const float* de1, const float* de2, uint32_t n,
+                           uint32_t width) {
+    DevBuf nodes, fnodes, tris;
+    uint32_t nn = 0, depth = 0;
+    bool fok = false;
+    if (int st = build_bvh_gpu(dv1, de1, de2, n, (uint32_t)kMaxLevels, (int)width, nodes, fnodes, tris, &nn, &depth,
+                               &fok, nullptr))
+        return st;
+    if (s->default_f32 && !fok)
+        return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
+    CRT_CUDA(cudaDeviceSynchronize());
+    s->nodes.swap(nodes);
+    s->fnodes.swap(fnodes);
+    s->tris.swap(tris);
+    s->bvh = Bvh8{};
+    s->bvh.fnodes_ok = fok;
+    s->bvh.max_depth = depth;
+    s->host_bvh = false;
+    s->dev.nodes = s->nodes.as<float4>();
+    s->dev.fnodes = fok ? s->fnodes.as<float4>() : nullptr;
+    s->dev.tris = s->tris.as<float4>();
+    crt_scene_info& I = s->info;
+    I.num_nodes = nn;
+    I.max_depth = depth;
+    I.node_bytes = (size_t)nn * (s->default_f32 ? sizeof(Bvh8FloatNode) : sizeof(Bvh8Node));
+    I.triangle_bytes = (size_t)n * sizeof(TriRecord);
+    I.bvh_width = width;
+    ++s->generation;
+    return CRT_OK;
+}
+
+// Builds the BVH of host arrays v1/e1/e2 ([n][3]) with the scene's builder and installs it.
 static int build_and_install(crt_scene s, const std::vector<float>& v1, const std::vector<float>& e1,
                              const std::vector<float>& e2, uint32_t n, uint32_t width) {
     if (s->builder == CRT_BVH_GPU) {
-        DevBuf dv1, de1, de2, nodes, fnodes, tris;
+        DevBuf dv1, de1, de2;
         int st = CRT_OK;
         if ((st = upload(dv1, v1)) || (st = upload(de1, e1)) || (st = upload(de2, e2))) return st;
-        uint32_t nn = 0, depth = 0;
-        bool fok = false;
-        if ((st = build_bvh_gpu(dv1.as<float>(), de1.as<float>(), de2.as<float>(), n, (uint32_t)kMaxLevels,
-                                (int)width, nodes, fnodes, tris, &nn, &depth, &fok, nullptr)))
-            return st;
-        if (s->default_f32 && !fok)
-            return set_error(CRT_ERR_LIMIT, "FP32 nodes hold 24-bit child indices; scene has more than 2^24 nodes");
-        CRT_CUDA(cudaDeviceSynchronize());
-        s->nodes.swap(nodes);
-        s->fnodes.swap(fnodes);
-        s->tris.swap(tris);
-        s->bvh = Bvh8{};
-        s->bvh.fnodes_ok = fok;
-        s->bvh.max_depth = depth;
-        s->host_bvh = false;
-        s->dev.nodes = s->nodes.as<float4>();
-        s->dev.fnodes = fok ? s->fnodes.as<float4>() : nullptr;
-        s->dev.tris = s->tris.as<float4>();
-        crt_scene_info& I = s->info;
-        I.num_nodes = nn;
-        I.max_depth = depth;
-        I.node_bytes = (size_t)nn * (s->default_f32 ? sizeof(Bvh8FloatNode) : sizeof(Bvh8Node));
-        I.triangle_bytes = (size_t)n * sizeof(TriRecord);
-        I.bvh_width = width;
-        ++s->generation;
-        return CRT_OK;
+        return build_on_device(s, dv1.as<float>(), de1.as<float>(), de2.as<float>(), n, width);
     }
     Bvh8 bvh;
     const char* msg = nullptr;
@@ -130,6 +140,78 @@ static int build_and_install(crt_scene s, const std::vector<float>& v1, const st
 inline float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
 inline float bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline float bits(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
+
+// Per-face records on the device, in the operation order of
+// Scene::loadTriangles (scene.cpp:111-130): v1, e1 = v2 - v1, e2 = v3 - v1
+// (or the edges as given), area = |e1 x e2| / 2; shading records (three
+// normals, area, material id) and uvs.
+__global__ void k_pack_faces(const float* __restrict__ pos, const float* __restrict__ nor,
+                             const float* __restrict__ uv, const uint32_t* __restrict__ mid, uint32_t n, bool edges,
+                             float* __restrict__ v1, float* __restrict__ e1, float* __restrict__ e2,
+                             float4* __restrict__ shade, float4* __restrict__ uvs) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* p = pos + 9ull * i;
+        float a[3], b[3];
+        for (int k = 0; k < 3; ++k) {
+            a[k] = edges ? p[3 + k] : p[3 + k] - p[k];
+            b[k] = edges ? p[6 + k] : p[6 + k] - p[k];
+            v1[3ull * i + k] = p[k];
+            e1[3ull * i + k] = a[k];
+            e2[3ull * i + k] = b[k];
+        }
+        const float cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+        const float area = sqrtf(cx * cx + cy * cy + cz * cz) / 2.0f;
+        const float* nn = nor + 9ull * i;
+        shade[3ull * i + 0] = make_float4(nn[0], nn[1], nn[2], nn[3]);
+        shade[3ull * i + 1] = make_float4(nn[4], nn[5], nn[6], nn[7]);
+        shade[3ull * i + 2] = make_float4(nn[8], area, __uint_as_float(mid[i]), 0.f);
+        if (uv) {
+            const float* t = uv + 6ull * i;
+            uvs[2ull * i + 0] = make_float4(t[0], t[1], t[2], t[3]);
+            uvs[2ull * i + 1] = make_float4(t[4], t[5], 0.f, 0.f);
+        } else {
+            uvs[2ull * i + 0] = uvs[2ull * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+// Texels to float4: linear floats as given, or RGBA8 through the 8-bit to
+// float table stbi_loadf applies; alpha dropped.
+__global__ void k_pack_texels(const float* __restrict__ rgb, const uchar4* __restrict__ rgba8,
+                              const float* __restrict__ table, uint64_t total, float4* __restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (rgba8) {
+            const uchar4 c = rgba8[i];
+            out[i] = make_float4(table[c.x], table[c.y], table[c.z], 0.f);
+        } else {
+            out[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.f);
+        }
+    }
+}
+
+// Face area on the host, in k_pack_faces' operation order.
+static float face_area(const crt_scene_desc* d, uint32_t f, float e1[3], float e2[3]) {
+    const bool edges = (d->flags & CRT_SCENE_EDGES) != 0;
+    const float* p = d->positions + 9ull * f;
+    for (int k = 0; k < 3; ++k) {
+        e1[k] = edges ? p[3 + k] : p[3 + k] - p[k];
+        e2[k] = edges ? p[6 + k] : p[6 + k] - p[k];
+    }
+    const float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                cz = e1[0] * e2[1] - e1[1] * e2[0];
+    return sqrtf(cx * cx + cy * cy + cz * cz) / 2.0f;
+}
+
+template <typename T>
+static int upload_raw(DevBuf& b, const T* p, size_t count) {
+    cudaError_t e = b.alloc(count ? count * sizeof(T) : 16);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMalloc");
+    if (count) {
+        e = cudaMemcpy(b.p, p, count * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_error(e, "cudaMemcpy");
+    }
+    return CRT_OK;
+}
 
 // Materials (createMaterialsData, parallel_renderer.cu:252-279) with the
 // emission scaling ka = Ka * 3 * lightsArea (scene.cpp:163,177).
@@ -205,7 +287,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
         if (d->materials[m].bsdf < 0 || d->materials[m].bsdf > CRT_BSDF_EMISSIVE)
             return set_error(CRT_ERR_INVALID, "unknown bsdf in material " + std::to_string(m));
     }
-    if (d->num_textures && (!d->texture_dims || !d->texels))
+    if (d->num_textures && (!d->texture_dims || (!d->texels && !d->texels_rgba8)))
         return set_error(CRT_ERR_INVALID, "textures need dims and texels");
     if (d->node_format > CRT_NODES_F32) return set_error(CRT_ERR_INVALID, "unknown node format");
     if (d->flags & ~(uint32_t)(CRT_SCENE_EDGES | CRT_SCENE_KA_SCALED))
@@ -217,22 +299,8 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     auto t0 = std::chrono::steady_clock::now();
     crt_scene s = new crt_scene_s();
 
-    // Triangle geometry as Scene::loadTriangles computes it (scene.cpp:111-130).
-    const bool edges = (d->flags & CRT_SCENE_EDGES) != 0;
-    std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n), area(n);
-    for (uint32_t i = 0; i < n; ++i) {
-        const float* p = d->positions + 9ull * i;
-        for (int k = 0; k < 3; ++k) {
-            v1[3 * i + k] = p[k];
-            e1[3 * i + k] = edges ? p[3 + k] : p[3 + k] - p[k];
-            e2[3 * i + k] = edges ? p[6 + k] : p[6 + k] - p[k];
-        }
-        const float* a = &e1[3 * i];
-        const float* b = &e2[3 * i];
-        float cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
-        area[i] = sqrtf(cx * cx + cy * cy + cz * cz) / 2.0f;
-    }
-    // Light list (scene.cpp:148-160) and total light area (scene.cpp:167-173).
+    // Light list (scene.cpp:148-160) and total light area (scene.cpp:167-173),
+    // with each light's geometry as Scene::loadTriangles computes it.
     if (d->num_lights) {
         if (!d->light_indices) { delete s; return set_error(CRT_ERR_INVALID, "light_indices is null"); }
         for (uint32_t i = 0; i < d->num_lights; ++i) {
@@ -247,42 +315,20 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
         delete s;
         return set_error(CRT_ERR_INVALID, "scene has no emissive triangles (light sampling needs one)");
     }
-    float lights_area = 0;
-    for (uint32_t f : s->lights) lights_area += area[f];
-    // Host-side validation is complete; from here on a device is needed.
-    cudaError_t dev_err = cudaGetDevice(&s->device);
-    if (dev_err != cudaSuccess) { delete s; return cuda_error(dev_err, "cudaGetDevice"); }
-
-    const uint32_t width = d->bvh_width ? d->bvh_width : 8u;
-    s->builder = d->builder;
-
-    // Per-face shading records.
-    std::vector<float4> shade(3ull * n), uvs(2ull * n);
-    for (uint32_t i = 0; i < n; ++i) {
-        const float* nn = d->normals + 9ull * i;
-        shade[3 * i + 0] = f4(nn[0], nn[1], nn[2], nn[3]);
-        shade[3 * i + 1] = f4(nn[4], nn[5], nn[6], nn[7]);
-        shade[3 * i + 2] = f4(nn[8], area[i], bits(d->material_ids[i]), 0.f);
-        if (d->uvs) {
-            const float* t = d->uvs + 6ull * i;
-            uvs[2 * i + 0] = f4(t[0], t[1], t[2], t[3]);
-            uvs[2 * i + 1] = f4(t[4], t[5], 0.f, 0.f);
-        } else {
-            uvs[2 * i + 0] = uvs[2 * i + 1] = f4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-    const std::vector<float4> mats =
-        pack_materials(d->materials, d->num_materials, lights_area, (d->flags & CRT_SCENE_KA_SCALED) != 0);
     std::vector<float4> lgeo(3 * s->lights.size());
+    float lights_area = 0;
     for (size_t i = 0; i < s->lights.size(); ++i) {
-        uint32_t f = s->lights[i];
-        lgeo[3 * i + 0] = f4(v1[3 * f], v1[3 * f + 1], v1[3 * f + 2], bits(f));
-        lgeo[3 * i + 1] = f4(e1[3 * f], e1[3 * f + 1], e1[3 * f + 2], area[f]);
-        lgeo[3 * i + 2] = f4(e2[3 * f], e2[3 * f + 1], e2[3 * f + 2], bits(d->material_ids[f]));
+        const uint32_t f = s->lights[i];
+        float e1[3], e2[3];
+        const float area = face_area(d, f, e1, e2);
+        const float* p = d->positions + 9ull * f;
+        lgeo[3 * i + 0] = f4(p[0], p[1], p[2], bits(f));
+        lgeo[3 * i + 1] = f4(e1[0], e1[1], e1[2], area);
+        lgeo[3 * i + 2] = f4(e2[0], e2[1], e2[2], bits(d->material_ids[f]));
+        lights_area += area;
     }
     // Textures flattened in order, then as many zero texels as the last
     // texture is wide (texture_store.cpp:68-70).
-    std::vector<float4> texels;
     std::vector<uint2> dims;
     std::vector<uint32_t> offs;
     uint64_t total = 0;
@@ -294,23 +340,83 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
         total += (uint64_t)w * h;
         if (total >= (1ull << 31)) { delete s; return set_error(CRT_ERR_LIMIT, "texture data too large"); }
     }
-    texels.reserve(total + (d->num_textures ? dims.back().x : 0));
-    for (uint64_t i = 0; i < total; ++i)
-        texels.push_back(f4(d->texels[3 * i], d->texels[3 * i + 1], d->texels[3 * i + 2], 0.f));
-    if (d->num_textures)
-        for (uint32_t i = 0; i < dims.back().x; ++i) texels.push_back(f4(0.f, 0.f, 0.f, 0.f));
+    const uint64_t pad = d->num_textures ? dims.back().x : 0;
+    // Host-side validation is complete; from here on a device is needed.
+    cudaError_t dev_err = cudaGetDevice(&s->device);
+    if (dev_err != cudaSuccess) { delete s; return cuda_error(dev_err, "cudaGetDevice"); }
 
-    int st = CRT_OK;
+    const uint32_t width = d->bvh_width ? d->bvh_width : 8u;
+    s->builder = d->builder;
     const bool f32 = d->node_format == CRT_NODES_F32;
     // Both encodings go to the device (the FP32 one only while child indices
     // fit 24 bits); each render picks one.
     s->default_f32 = f32;
     s->n_mats = d->num_materials;
     s->ka_scaled = (d->flags & CRT_SCENE_KA_SCALED) != 0;
-    if ((st = build_and_install(s, v1, e1, e2, n, width)) ||
-        (st = upload(s->shade, shade)) || (st = upload(s->uvs, uvs)) || (st = upload(s->mats, mats)) ||
-        (st = upload(s->light_geo, lgeo)) || (st = upload(s->texels, texels)) ||
-        (st = upload(s->tex_dims, dims)) || (st = upload(s->tex_offsets, offs))) {
+
+    // The caller's arrays go up as they are; one kernel forms the triangle,
+    // shading and uv records there.
+    int st = CRT_OK;
+    {
+        DevBuf dpos, dnor, duv, dmid, dv1, de1, de2;
+        if ((st = upload_raw(dpos, d->positions, 9ull * n)) || (st = upload_raw(dnor, d->normals, 9ull * n)) ||
+            (d->uvs && (st = upload_raw(duv, d->uvs, 6ull * n))) || (st = upload_raw(dmid, d->material_ids, n))) {
+            delete s;
+            return st;
+        }
+        cudaError_t e = dv1.alloc(12ull * n);
+        if (e == cudaSuccess) e = de1.alloc(12ull * n);
+        if (e == cudaSuccess) e = de2.alloc(12ull * n);
+        if (e == cudaSuccess) e = s->shade.alloc(48ull * n);
+        if (e == cudaSuccess) e = s->uvs.alloc(32ull * n);
+        if (e != cudaSuccess) { delete s; return cuda_error(e, "cudaMalloc"); }
+        const uint32_t grid = (uint32_t)std::min<uint64_t>((n + 255) / 256, 4096);
+        k_pack_faces<<<grid, 256>>>(dpos.as<float>(), dnor.as<float>(), d->uvs ? duv.as<float>() : nullptr,
+                                    dmid.as<uint32_t>(), n, (d->flags & CRT_SCENE_EDGES) != 0, dv1.as<float>(),
+                                    de1.as<float>(), de2.as<float>(), s->shade.as<float4>(), s->uvs.as<float4>());
+        e = cudaGetLastError();
+        if (e != cudaSuccess) { delete s; return cuda_error(e, "k_pack_faces"); }
+        if (s->builder == CRT_BVH_GPU) {
+            st = build_on_device(s, dv1.as<float>(), de1.as<float>(), de2.as<float>(), n, width);
+        } else {
+            std::vector<float> v1(3ull * n), e1(3ull * n), e2(3ull * n);
+            e = cudaMemcpy(v1.data(), dv1.p, 12ull * n, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess) e = cudaMemcpy(e1.data(), de1.p, 12ull * n, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess) e = cudaMemcpy(e2.data(), de2.p, 12ull * n, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) { delete s; return cuda_error(e, "cudaMemcpy"); }
+            st = build_and_install(s, v1, e1, e2, n, width);
+        }
+        if (st != CRT_OK) { delete s; return st; }
+    }
+    {   // texels: floats or RGBA8 bytes up, float4 records formed on the device
+        DevBuf raw, table;
+        cudaError_t e = s->texels.alloc(16ull * (total + pad) + (total + pad == 0 ? 16 : 0));
+        if (e == cudaSuccess && pad) e = cudaMemset(s->texels.as<float4>() + total, 0, 16ull * pad);
+        if (e != cudaSuccess) { delete s; return cuda_error(e, "texels"); }
+        if (total) {
+            if (d->texels_rgba8) {
+                if ((st = upload_raw(raw, d->texels_rgba8, 4ull * total)) ||
+                    (st = upload_raw(table, stb_texel_table(), 256))) {
+                    delete s;
+                    return st;
+                }
+            } else if ((st = upload_raw(raw, d->texels, 3ull * total))) {
+                delete s;
+                return st;
+            }
+            const uint32_t grid = (uint32_t)std::min<uint64_t>((total + 255) / 256, 4096);
+            k_pack_texels<<<grid, 256>>>(d->texels_rgba8 ? nullptr : raw.as<float>(),
+                                         d->texels_rgba8 ? raw.as<uchar4>() : nullptr, table.as<float>(), total,
+                                         s->texels.as<float4>());
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) { delete s; return cuda_error(e, "k_pack_texels"); }
+        }
+    }
+    const std::vector<float4> mats =
+        pack_materials(d->materials, d->num_materials, lights_area, (d->flags & CRT_SCENE_KA_SCALED) != 0);
+    if ((st = upload(s->mats, mats)) || (st = upload(s->light_geo, lgeo)) || (st = upload(s->tex_dims, dims)) ||
+        (st = upload(s->tex_offsets, offs))) {
         delete s;
         return st;
     }
@@ -326,7 +432,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     D.texels = s->texels.as<float4>();
     D.tex_dims = s->tex_dims.as<uint2>();
     D.tex_offsets = s->tex_offsets.as<uint32_t>();
-    D.tex_total = (uint32_t)texels.size();
+    D.tex_total = (uint32_t)(total + pad);
     D.n_lights = (uint32_t)s->lights.size();
     D.lights_area = lights_area;
     D.n_faces = n;
@@ -337,8 +443,8 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     I.num_lights = D.n_lights;
     I.num_materials = d->num_materials;
     I.num_textures = d->num_textures;
-    I.shading_bytes = (shade.size() + uvs.size()) * sizeof(float4);
-    I.texture_bytes = texels.size() * sizeof(float4);
+    I.shading_bytes = 80ull * n;   // 3 + 2 float4 per face
+    I.texture_bytes = 16ull * (total + pad);
     I.lights_area = lights_area;
     I.build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     *out = s;

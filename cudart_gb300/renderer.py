@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib
 from ._lib import (Camera, Material, RenderOptions, SceneDesc, SceneInfo, TuneParams, TuneResult,
                    View, check, load)
-from .scenes import NO_TEXTURE, SceneArrays, texture_texels
+from .scenes import NO_TEXTURE, SceneArrays
 
 NODE_DT = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base", "<u4"),
                     ("tri_base", "<u4"), ("meta", "u1", 8), ("qlo", "u1", (3, 8)),
@@ -57,6 +57,14 @@ def bvh_build_host(positions: np.ndarray, width: int = 8):
 
 
 NODE_FORMATS = {"q8": _lib.NODES_Q8, "f32": _lib.NODES_F32}
+
+
+def _rgba8(img: np.ndarray) -> np.ndarray:
+    """uint8 [h, w, 3 or 4] image -> flat RGBA8 bytes."""
+    img = np.asarray(img, np.uint8)
+    if img.shape[2] == 3:
+        img = np.concatenate([img, np.full(img.shape[:2] + (1,), 255, np.uint8)], axis=2)
+    return np.ascontiguousarray(img[..., :4]).reshape(-1)
 
 
 def _face_areas(e1: np.ndarray, e2: np.ndarray) -> np.ndarray:
@@ -132,18 +140,19 @@ class GB300Scene:
         else:
             mats = _material_table(sc.materials)
         dims = np.asarray([d for img in sc.textures for d in (img.shape[1], img.shape[0])], np.uint32)
-        texels = (np.concatenate([texture_texels(img) for img in sc.textures]).astype(np.float32)
-                  if sc.textures else np.zeros((1, 3), np.float32))
+        # RGBA8 texels, converted on the device as stbi_loadf converts them
+        rgba = (np.concatenate([_rgba8(img) for img in sc.textures]) if sc.textures
+                else np.zeros(4, np.uint8))
         li = (np.ascontiguousarray(lights, np.uint32) if lights is not None
               else np.zeros(1, np.uint32))
-        self._keep += [pos, nor, uvs, mid, mats, dims, texels, li]
+        self._keep += [pos, nor, uvs, mid, mats, dims, rgba, li]
         desc = SceneDesc(sc.n_tris, pos.ctypes.data, nor.ctypes.data, uvs.ctypes.data,
                          mid.ctypes.data, len(sc.materials), C.addressof(mats),
                          len(lights) if lights is not None else 0,
                          li.ctypes.data if lights is not None else None,
                          len(sc.textures), dims.ctypes.data if len(dims) else None,
-                         texels.ctypes.data, NODE_FORMATS[node_format], bvh_width, flags,
-                         builder_id)
+                         None, NODE_FORMATS[node_format], bvh_width, flags, builder_id,
+                         rgba.ctypes.data if sc.textures else None)
         h = C.c_void_p()
         check(L.crt_scene_create(C.byref(desc), C.byref(h)))
         self.handle = h

@@ -106,12 +106,16 @@ typedef struct {
     uint32_t num_textures;
     const uint32_t* texture_dims;  /* [num_textures][width, height] */
     const float* texels;           /* [sum(w*h)][rgb] linear floats, as
-                                      stbi_loadf returns them */
+                                      stbi_loadf returns them (or NULL with
+                                      texels_rgba8) */
     uint32_t node_format;          /* crt_node_format renders use by default; both
                                       encodings are uploaded */
     uint32_t bvh_width;            /* children per node: 4 or 8 (0 = 8) */
     uint32_t flags;                /* crt_scene_flags */
     uint32_t builder;              /* crt_bvh_builder */
+    const uint8_t* texels_rgba8;   /* instead of texels: [sum(w*h)][rgba] bytes,
+                                      converted on the device as stbi_loadf
+                                      converts 8-bit data (alpha dropped) */
 } crt_scene_desc;
 
 /* Inputs as the reference's Scene holds them after construction, so a
@@ -129,9 +133,10 @@ typedef enum {
 typedef enum {
     CRT_BVH_HOST = 0u,   /* binned SAH (32 bins; exact sweep below 33 triangles),
                             host threads: the best trees */
-    CRT_BVH_GPU = 1u     /* linear BVH over 63-bit Morton codes (Karras 2012) on
-                            the device, then the same collapse and encoding:
-                            tens of milliseconds for millions of triangles */
+    CRT_BVH_GPU = 1u     /* PLOC clustering (Meister and Bittner 2018) over
+                            63-bit Morton order on the device, then the same
+                            collapse and encoding: a few milliseconds for
+                            millions of triangles */
 } crt_bvh_builder;
 
 /* BVH node encoding on the device (same tree either way). */
