@@ -2,6 +2,7 @@
 #include "bvh8.h"
 
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -33,20 +34,23 @@ struct Box {
 
 struct Node2 {
     Box box;
-    int32_t left, right;     // children (internal)
-    uint32_t first, count;   // leaf range into the index array (count > 0)
+    int32_t left, right;     // children; -1 for a leaf
+    uint32_t first, count;   // range of the index array the node covers
 };
 
 constexpr int kBins = 32;
 constexpr uint32_t kSmallMax = 32;        // ranges up to this size get an exact SAH sweep
-// Largest leaf of the binary build.  The reference stops at 3 (maxTrisInNode,
-// bvh.cpp:62); 2 costs ~2% more nodes and traces ~2% faster on the 8-wide
-// layout (fewer triangle tests per visited leaf slot).  The leaf encoding
-// allows up to 3.
-#ifndef CRT_LEAF_MAX
-#define CRT_LEAF_MAX 2
-#endif
-constexpr uint32_t kLeafMax = CRT_LEAF_MAX;
+// The binary build goes down to single triangles; the collapse to wide nodes
+// is SAH-optimal by dynamic programming over that tree (Ylitie, Karras and
+// Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+// BVHs", HPG 2017) and also decides which subtrees of at most 3 triangles
+// become leaf slots.  The triangle test costs 0.5 of a wide-node visit in
+// the cost model (0.2 / 0.3 / 0.5 / 1.0 measured on C2 and C3: 0.5 fastest).
+// Against the earlier greedy collapse (open the largest-area child, leaves
+// of 2) it traces 4% faster with 37% fewer nodes.
+constexpr uint32_t kLeafMax = 1;
+constexpr uint32_t kSlotTrisMax = 3;   // triangles a leaf slot holds (3-bit count)
+constexpr float kTriCost = 0.5f;
 constexpr uint32_t kParallelMin = 1u << 15;
 
 struct Builder {
@@ -240,18 +244,16 @@ struct Builder {
         }
         Node2& me = nodes[slot];
         me.box = nb;
+        me.first = start;
+        me.count = end - start;
         if (end - start <= kLeafMax) {
             me.left = me.right = -1;
-            me.first = start;
-            me.count = end - start;
             return;
         }
         const uint32_t mid = split(start, end, cb);
         const uint32_t lslot = slot + 1, rslot = slot + 2 * (mid - start);
         me.left = (int32_t)lslot;
         me.right = (int32_t)rslot;
-        me.first = 0;
-        me.count = 0;
         if (par_depth > 0 && end - start >= kParallelMin) {
             auto fut = std::async(std::launch::async, [&] { build(start, mid, nodes, lslot, par_depth - 1); });
             build(mid, end, nodes, rslot, par_depth - 1);
@@ -291,6 +293,100 @@ int scale_exponent(double ext) {
 }
 
 }  // namespace
+
+// SAH-optimal collapse of a binary tree into nodes of at most W children
+// (Ylitie et al. 2017, section 4): with C(x, i) the least SAH cost of the
+// subtree of x as at most i slots,
+//   C(x, 1) = min(c_tri * A(x) * N(x)  [x a leaf slot, N(x) <= 3],
+//                 A(x) + D(x, W)       [x a wide node]),
+//   C(x, i) = min(C(x, i - 1), D(x, i)),  D(x, i) = min_k C(l, k) + C(r, i - k),
+// computed bottom-up (subtrees in parallel); the decisions then give each
+// wide node its children.
+struct DpCollapse {
+    struct Dec {
+        uint8_t leaf;        // as one slot: a leaf slot (else a wide node)
+        uint8_t wk;          // as a wide node: slots of the left child
+        uint8_t split[9];    // with at most i slots (i >= 2): slots of the left child, 0 = as with i - 1
+    };
+    using Costs = std::array<float, 9>;
+    const Node2* n2;
+    std::vector<Dec> dec;
+    int W;
+    float ctri;
+
+    Costs run(int32_t x, int par_depth) {
+        const Node2& nd = n2[x];
+        const float A = nd.box.half_area();
+        const float leafc = nd.count <= kSlotTrisMax ? ctri * A * (float)nd.count : FLT_MAX;
+        Dec& d = dec[x];
+        Costs C;
+        C[0] = 0.f;
+        if (nd.left < 0) {
+            for (int i = 1; i <= W; ++i) {
+                C[i] = leafc;
+                d.split[i] = 0;
+            }
+            d.leaf = 1;
+            d.wk = 0;
+            return C;
+        }
+        Costs L, R;
+        if (par_depth > 0 && nd.count >= kParallelMin) {
+            auto fut = std::async(std::launch::async, [&] { return run(nd.left, par_depth - 1); });
+            R = run(nd.right, par_depth - 1);
+            L = fut.get();
+        } else {
+            L = run(nd.left, 0);
+            R = run(nd.right, 0);
+        }
+        float D[9];
+        uint8_t K[9];
+        for (int i = 2; i <= W; ++i) {
+            D[i] = FLT_MAX;
+            K[i] = 1;
+            for (int k = 1; k < i; ++k) {
+                const float c = L[k] + R[i - k];
+                if (c < D[i]) {
+                    D[i] = c;
+                    K[i] = (uint8_t)k;
+                }
+            }
+        }
+        const float wide = A + D[W];
+        d.leaf = leafc <= wide;
+        d.wk = K[W];
+        C[1] = d.leaf ? leafc : wide;
+        d.split[1] = 0;
+        for (int i = 2; i <= W; ++i) {
+            if (D[i] < C[i - 1]) {
+                C[i] = D[i];
+                d.split[i] = K[i];
+            } else {
+                C[i] = C[i - 1];
+                d.split[i] = 0;
+            }
+        }
+        return C;
+    }
+    // The slots of the subtree of x when it may use at most i of them.
+    void expand(int32_t x, int i, int32_t* out, int& n) const {
+        while (i > 1 && dec[x].split[i] == 0) --i;
+        if (i == 1) {
+            out[n++] = x;
+            return;
+        }
+        const int k = dec[x].split[i];
+        expand(n2[x].left, k, out, n);
+        expand(n2[x].right, i - k, out, n);
+    }
+    // Children of the wide node at x.
+    int children(int32_t x, int32_t* out) const {
+        int n = 0;
+        expand(n2[x].left, dec[x].wk, out, n);
+        expand(n2[x].right, W - dec[x].wk, out, n);
+        return n;
+    }
+};
 
 bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
                 uint32_t max_levels, Bvh8& out, const char** msg, int max_children) {
@@ -337,10 +433,15 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
     while ((1u << par_depth) < hw * 2 && par_depth < 8) ++par_depth;
     b.build(0, n, n2_store.get(), 0, par_depth);
     const int32_t root = 0;
+    DpCollapse dp{n2, {}, max_children, kTriCost};
+    dp.dec.resize(2ull * n - 1);
+    dp.run(root, par_depth);
+    // a slot of a wide node is a leaf slot or another wide node
+    auto leaf_slot = [&](int32_t x) { return dp.dec[x].leaf != 0; };
 
     // ---- collapse to max_children-wide nodes, breadth-first layout --------
-    // 1. (serial, cheap) each wide node takes its BVH2 node's children and
-    //    keeps opening the internal child of largest area;
+    // 1. (serial, cheap) each wide node takes the children the SAH-optimal
+    //    collapse chose;
     // 2. (parallel) children are assigned to slots by octant;
     // 3. (serial, cheap) breadth-first numbering in slot order gives each
     //    node its child and triangle base;
@@ -360,24 +461,10 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
         w.depth = depth;
         int32_t* ch = w.ch;
         int nch = 0;
-        if (n2[node2].count > 0) {
+        if (leaf_slot(node2)) {
             ch[nch++] = node2;                 // single-leaf root
         } else {
-            ch[nch++] = n2[node2].left;
-            ch[nch++] = n2[node2].right;
-            while (nch < max_children) {
-                int best = -1;
-                float area = -1.f;
-                for (int c = 0; c < nch; ++c)
-                    if (n2[ch[c]].count == 0 && n2[ch[c]].box.half_area() > area) {
-                        area = n2[ch[c]].box.half_area();
-                        best = c;
-                    }
-                if (best < 0) break;
-                int32_t x = ch[best];
-                ch[best] = n2[x].left;
-                ch[nch++] = n2[x].right;
-            }
+            nch = dp.children(node2, ch);
         }
         w.nch = nch;
         recs.push_back(w);
@@ -390,7 +477,7 @@ bool build_bvh8(const float* v1, const float* e1, const float* e2, uint32_t n,
         if (depth > max_levels) { *msg = "BVH deeper than the traversal stack allows"; return false; }
         for (int c = 0; c < recs[r].nch; ++c) {
             const int32_t x = recs[r].ch[c];
-            if (n2[x].count == 0) {
+            if (!leaf_slot(x)) {
                 recs[r].rec[c] = (int32_t)recs.size();
                 add_record(x, depth + 1);
             } else {

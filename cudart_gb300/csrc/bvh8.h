@@ -2,10 +2,12 @@
 //
 // Replaces the reference's binary SAH build (src/geometry/bvh.cpp:65-323,
 // 32-byte LinearBVHNode, two 1-D textures on the GPU) with:
-//   1. a binned surface-area-heuristic binary build (leaves of <= 2
-//      triangles; the reference's maxTrisInNode is 3, bvh.cpp:62);
-//   2. a greedy collapse to 8-wide nodes (open the child with the largest
-//      surface area until 8 children);
+//   1. a binned surface-area-heuristic binary build down to single
+//      triangles (exact SAH sweep for ranges of at most 32);
+//   2. an SAH-optimal collapse to 8-wide (or 4-wide) nodes by dynamic
+//      programming (Ylitie et al., HPG 2017), which also groups triangles
+//      into leaf slots of at most 3 (the reference's maxTrisInNode,
+//      bvh.cpp:62);
 //   3. child slots ordered by octant so that visiting slot k ^ octant(ray)
 //      is approximately front to back;
 //   4. child boxes quantised to 8 bits per plane relative to the node
