@@ -8,10 +8,12 @@
 // order, the one whose merged box has the least surface area; mutual
 // nearest neighbours merge (the merged cluster keeps the left one's place),
 // and the list is compacted.  Then the host build's collapse and encoding
-// (bvh8.cpp) run level by level: each wide node opens its largest-area
-// internal children until it has 8 (or 4), assigns them to slots by octant,
-// and quantises their boxes outward on a power-of-two grid.  A subtree of at
-// most kLeafMaxGpu triangles becomes a leaf slot.  Node and triangle layouts
+// (bvh8.cpp) run level by level: each wide node takes the children the
+// collapse chose, assigns them to slots by octant, and quantises their boxes
+// outward on a power-of-two grid.  The collapse is
+// the host build's SAH-optimal dynamic programme (Ylitie et al., HPG 2017),
+// computed bottom-up on the device; it also picks the leaf slots (subtrees
+// of at most 3 triangles).  Node and triangle layouts
 // are the host build's, so the traversal kernels and every query result are
 // unchanged; only the tree differs, and with it the nodes a ray visits.
 //
@@ -30,15 +32,10 @@
 namespace crt {
 namespace {
 
-#ifndef CRT_GPU_LEAF_MAX
-#define CRT_GPU_LEAF_MAX 2             // as the host build's leaves
-#endif
-#ifndef CRT_PLOC_RADIUS
-#define CRT_PLOC_RADIUS 16             // PLOC search radius (clusters on each side)
-#endif
-constexpr uint32_t kLeafMaxGpu = CRT_GPU_LEAF_MAX;
+constexpr uint32_t kSlotTrisMax = 3;  // triangles a leaf slot holds (3-bit count)
+constexpr float kTriCost = 0.5f;      // the collapse's cost model, as the host build's
 constexpr int kBlock = 256;
-constexpr int kRadius = CRT_PLOC_RADIUS;
+constexpr int kRadius = 16;           // PLOC search radius (clusters on each side)
 
 struct GBox {
     float lo[3], hi[3];
@@ -51,6 +48,16 @@ struct GNode {
     GBox box;
     int32_t left, right, parent;
     uint32_t first, count;
+};
+
+// Decisions of the SAH-optimal collapse for one binary node (as DpCollapse
+// in bvh8.cpp): as one slot, a leaf slot or a wide node; as a wide node,
+// the slots of its left child; with at most i slots, those of the left
+// child (0: as with i - 1).
+struct GDec {
+    uint8_t leaf, wk;
+    uint8_t split[9];
+    uint8_t pad;
 };
 
 // Children of one wide node, in the order the collapse picked them.
@@ -132,17 +139,21 @@ __device__ __forceinline__ uint64_t spread21(uint64_t x) {
 // 63-bit Morton codes (21 bits per axis) of the centroids.
 __global__ void k_morton(const float* __restrict__ cent, uint32_t n, const uint32_t* __restrict__ cbounds,
                          uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
-    float lo[3], sc[3];
+    // one scale for all axes (the centroid bounds' largest extent): Morton
+    // cells are cubes, so a flat axis does not get the same weight in the
+    // curve as the wide ones
+    float lo[3];
     const float top = (float)((1u << 21) - 1u);
+    float ext = 0.f;
     for (int k = 0; k < 3; ++k) {
         lo[k] = order_float(cbounds[k]);
-        const float ext = order_float(cbounds[3 + k]) - lo[k];
-        sc[k] = ext > 0.f ? top / ext : 0.f;
+        ext = fmaxf(ext, order_float(cbounds[3 + k]) - lo[k]);
     }
+    const float sc = ext > 0.f ? top / ext : 0.f;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         uint64_t q[3];
         for (int k = 0; k < 3; ++k) {
-            const float f = (cent[3ull * t + k] - lo[k]) * sc[k];
+            const float f = (cent[3ull * t + k] - lo[k]) * sc;
             q[k] = (uint64_t)fminf(fmaxf(f, 0.f), top);
         }
         keys[t] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
@@ -263,34 +274,123 @@ __global__ void k_ploc_merge(const int32_t* __restrict__ clusters, const int32_t
     out[pos] = id;
 }
 
-__device__ __forceinline__ bool opens(const GNode& nd) { return nd.count > kLeafMaxGpu; }
+// C(x, 1..W) of the collapse, from the children's costs (cost[8 * node + i - 1]).
+__device__ void dp_node(int32_t x, const GNode& nd, const float* L, const float* R, int W, float* C, GDec& d) {
+    const float A = half_area(nd.box);
+    const float leafc = nd.count <= kSlotTrisMax ? kTriCost * A * (float)nd.count : FLT_MAX;
+    float D[9];
+    uint8_t K[9];
+    for (int i = 2; i <= W; ++i) {
+        D[i] = FLT_MAX;
+        K[i] = 1;
+        for (int k = 1; k < i; ++k) {
+            const float c = L[k - 1] + R[i - k - 1];
+            if (c < D[i]) {
+                D[i] = c;
+                K[i] = (uint8_t)k;
+            }
+        }
+    }
+    const float wide = A + D[W];
+    d.leaf = leafc <= wide;
+    d.wk = K[W];
+    C[0] = d.leaf ? leafc : wide;
+    d.split[1] = 0;
+    for (int i = 2; i <= W; ++i) {
+        if (D[i] < C[i - 2]) {
+            C[i - 1] = D[i];
+            d.split[i] = K[i];
+        } else {
+            C[i - 1] = C[i - 2];
+            d.split[i] = 0;
+        }
+    }
+}
 
-// One wide node per thread: children by largest area, slots by octant.
+__global__ void k_dp_leaves(int n, const GNode* __restrict__ nodes, int W, float* __restrict__ cost,
+                            GDec* __restrict__ dec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = n - 1 + i;
+    const float c = kTriCost * half_area(nodes[x].box) * (float)nodes[x].count;
+    for (int k = 0; k < W; ++k) cost[8ull * x + k] = c;
+    GDec d;
+    memset(&d, 0, sizeof(d));
+    d.leaf = 1;
+    dec[x] = d;
+}
+
+// Bottom-up: the second child to finish computes its parent.
+__global__ void k_dp_up(int n, const GNode* __restrict__ nodes, int W, float* cost, GDec* __restrict__ dec,
+                        uint32_t* flags, uint32_t* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = nodes[n - 1 + i].parent;
+    for (int climbed = 0; p >= 0; ++climbed) {
+        if (p > n - 2 || climbed >= n) {   // never expected; ends the climb
+            atomicOr(err, 8u);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[p], 1u) == 0) return;   // the sibling subtree is not done yet
+        __threadfence();
+        const GNode nd = nodes[p];
+        if (nd.left < 0 || nd.right < 0 || nd.left > 2 * n - 2 || nd.right > 2 * n - 2) {
+            atomicOr(err, 8u);
+            return;
+        }
+        float L[8], R[8], C[8];
+        for (int k = 0; k < W; ++k) {
+            L[k] = __ldcg(&cost[8ull * nd.left + k]);
+            R[k] = __ldcg(&cost[8ull * nd.right + k]);
+        }
+        GDec d;
+        memset(&d, 0, sizeof(d));
+        dp_node(p, nd, L, R, W, C, d);
+        for (int k = 0; k < W; ++k) __stcg(&cost[8ull * p + k], C[k]);
+        dec[p] = d;
+        p = nd.parent;
+    }
+}
+
+__device__ __forceinline__ bool wide_slot(const GDec* dec, int32_t x) { return dec[x].leaf == 0; }
+
+// One wide node per thread: the collapse's children, slots by octant.
 __global__ void k_choose(const int32_t* __restrict__ front, uint32_t F, const GNode* __restrict__ nodes,
-                         int max_children, GWide* __restrict__ recs, uint32_t* __restrict__ cnt_int,
-                         uint32_t* __restrict__ cnt_tri) {
+                         const GDec* __restrict__ dec, int max_children, GWide* __restrict__ recs,
+                         uint32_t* __restrict__ cnt_int, uint32_t* __restrict__ cnt_tri, int n, uint32_t* err) {
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     const int32_t x = front[f];
     GWide w;
     int nch = 0;
-    if (!opens(nodes[x])) {
+    if (!wide_slot(dec, x)) {
         w.ch[nch++] = x;                      // a root of at most 3 triangles
     } else {
-        w.ch[nch++] = nodes[x].left;
-        w.ch[nch++] = nodes[x].right;
-        while (nch < max_children) {
-            int best = -1;
-            float area = -1.f;
-            for (int c = 0; c < nch; ++c)
-                if (opens(nodes[w.ch[c]]) && half_area(nodes[w.ch[c]].box) > area) {
-                    area = half_area(nodes[w.ch[c]].box);
-                    best = c;
-                }
-            if (best < 0) break;
-            const int32_t y = w.ch[best];
-            w.ch[best] = nodes[y].left;
-            w.ch[nch++] = nodes[y].right;
+        // expand (node, slots) pairs left to right, as DpCollapse::expand
+        int32_t sn[16];
+        int sb[16];
+        int sp = 0;
+        sn[sp] = nodes[x].right;
+        sb[sp++] = max_children - dec[x].wk;
+        sn[sp] = nodes[x].left;
+        sb[sp++] = dec[x].wk;
+        while (sp > 0) {
+            const int32_t y = sn[--sp];
+            int i = sb[sp];
+            if (y < 0 || y > 2 * n - 2 || i < 1 || i > max_children) { atomicOr(err, 16u); break; }
+            while (i > 1 && dec[y].split[i] == 0) --i;
+            if (i == 1) {
+                if (nch < max_children) w.ch[nch++] = y;
+                else { atomicOr(err, 16u); break; }
+            } else {
+                const int k = dec[y].split[i];
+                if (sp + 2 > 16 || k < 1 || k >= i) { atomicOr(err, 16u); break; }
+                sn[sp] = nodes[y].right;
+                sb[sp++] = i - k;
+                sn[sp] = nodes[y].left;
+                sb[sp++] = k;
+            }
         }
     }
     w.nch = nch;
@@ -321,7 +421,7 @@ __global__ void k_choose(const int32_t* __restrict__ front, uint32_t F, const GN
     }
     uint32_t ni = 0, nt = 0;
     for (int c = 0; c < nch; ++c) {
-        if (opens(nodes[w.ch[c]])) ++ni;
+        if (wide_slot(dec, w.ch[c])) ++ni;
         else nt += nodes[w.ch[c]].count;
     }
     recs[f] = w;
@@ -342,7 +442,7 @@ __device__ int scale_exponent_d(double ext) {
 __global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t level_base, uint32_t next_base,
                        uint32_t tri_level_base, const uint32_t* __restrict__ int_off,
                        const uint32_t* __restrict__ tri_off, const GNode* __restrict__ nodes,
-                       const uint32_t* __restrict__ perm, const float* __restrict__ v1,
+                       const GDec* __restrict__ dec, const uint32_t* __restrict__ perm, const float* __restrict__ v1,
                        const float* __restrict__ e1, const float* __restrict__ e2, Bvh8Node* __restrict__ out,
                        Bvh8FloatNode* __restrict__ fout, TriRecord* __restrict__ tris, int32_t* __restrict__ next_front,
                        uint32_t n_tris, uint32_t cap_nodes, uint32_t* err) {
@@ -395,7 +495,7 @@ __global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t leve
             node.qlo[k][s] = (uint8_t)fmax(0.0, fmin(255.0, lo));
             node.qhi[k][s] = (uint8_t)fmax(0.0, fmin(255.0, hi));
         }
-        if (opens(cn)) {
+        if (wide_slot(dec, w.ch[c])) {
             node.imask |= (uint8_t)(1u << s);
             node.meta[s] = 0x80;
             const uint32_t k = int_off[f] + int_o++;
@@ -403,10 +503,10 @@ __global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t leve
             else atomicOr(err, 2u);
         } else {
             node.meta[s] = (uint8_t)((cn.count << 5) | tri_o);
-            // the subtree's triangles, left to right (at most kLeafMaxGpu)
-            uint32_t pos[kLeafMaxGpu];
+            // the subtree's triangles, left to right (at most kSlotTrisMax)
+            uint32_t pos[kSlotTrisMax];
             uint32_t np = 0;
-            int32_t stack[2 * kLeafMaxGpu];
+            int32_t stack[2 * kSlotTrisMax];
             int sp = 0;
             stack[sp++] = w.ch[c];
             while (sp > 0) {
@@ -414,9 +514,9 @@ __global__ void k_emit(const GWide* __restrict__ recs, uint32_t F, uint32_t leve
                 if (x < 0 || x > 2 * (int32_t)n_tris - 2) { atomicOr(err, 4u); break; }
                 const GNode& g = nodes[x];
                 if (g.left < 0) {
-                    if (np < kLeafMaxGpu) pos[np++] = g.first;
+                    if (np < kSlotTrisMax) pos[np++] = g.first;
                     else atomicOr(err, 4u);
-                } else if (sp + 2 <= 2 * (int)kLeafMaxGpu) {
+                } else if (sp + 2 <= 2 * (int)kSlotTrisMax) {
                     stack[sp++] = g.right;
                     stack[sp++] = g.left;
                 } else {
@@ -540,6 +640,16 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
         CRT_CUDA(cudaStreamSynchronize(s));
         if (root != 0 || next_id != -1) return set_error(CRT_ERR_CUDA, "GPU BVH build: clustering left no single root");
     }
+    // the collapse's costs and decisions, bottom-up
+    DevBuf dp_cost, dp_dec, dp_flags;
+    CRT_CUDA(dp_cost.alloc((size_t)(2 * n - 1) * 8 * sizeof(float)));
+    CRT_CUDA(dp_dec.alloc((size_t)(2 * n - 1) * sizeof(GDec)));
+    CRT_CUDA(dp_flags.alloc((size_t)n * 4));
+    CRT_CUDA(cudaMemsetAsync(dp_flags.p, 0, (size_t)n * 4, s));
+    k_dp_leaves<<<blocks(n), kBlock, 0, s>>>(ni, gn, max_children, dp_cost.as<float>(), dp_dec.as<GDec>());
+    k_dp_up<<<blocks(n), kBlock, 0, s>>>(ni, gn, max_children, dp_cost.as<float>(), dp_dec.as<GDec>(),
+                                         dp_flags.as<uint32_t>(), err);
+    const GDec* dec = dp_dec.as<GDec>();
     CRT_CUDA(cudaGetLastError());
     {   // the collapse follows child links: stop here if any were not set
         uint32_t e = 0;
@@ -571,8 +681,8 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
     int32_t* nxt = front_b.as<int32_t>();
     while (F > 0) {
         if (++depth > max_levels) return set_error(CRT_ERR_LIMIT, "BVH deeper than the traversal stack allows");
-        k_choose<<<blocks(F), kBlock, 0, s>>>(cur, F, gn, max_children, recs.as<GWide>(), cnt_int.as<uint32_t>(),
-                                              cnt_tri.as<uint32_t>());
+        k_choose<<<blocks(F), kBlock, 0, s>>>(cur, F, gn, dec, max_children, recs.as<GWide>(), cnt_int.as<uint32_t>(),
+                                              cnt_tri.as<uint32_t>(), ni, err);
         // exclusive sums over F + 1 entries: the last is each level's total
         CRT_CUDA(cudaMemsetAsync(cnt_int.as<uint32_t>() + F, 0, 4, s));
         CRT_CUDA(cudaMemsetAsync(cnt_tri.as<uint32_t>() + F, 0, 4, s));
@@ -582,7 +692,7 @@ int build_bvh_gpu(const float* d_v1, const float* d_e1, const float* d_e2, uint3
                                                (int)F + 1, s));
         const uint32_t next_base = level_base + F;
         k_emit<<<blocks(F), kBlock, 0, s>>>(recs.as<GWide>(), F, level_base, next_base, tri_base,
-                                            off_int.as<uint32_t>(), off_tri.as<uint32_t>(), gn, perm.as<uint32_t>(),
+                                            off_int.as<uint32_t>(), off_tri.as<uint32_t>(), gn, dec, perm.as<uint32_t>(),
                                             d_v1, d_e1, d_e2, nodes_out.as<Bvh8Node>(), fnodes_out.as<Bvh8FloatNode>(),
                                             tris_out.as<TriRecord>(), nxt, n, cap_nodes, err);
         uint32_t totals[2];
