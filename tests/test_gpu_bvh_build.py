@@ -47,7 +47,11 @@ def test_gpu_tree_degenerate_inputs(cuda):
     one = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]]], np.float32)
     rng = np.random.default_rng(0)
     tiny = rng.uniform(-1, 1, (500, 1, 3)).astype(np.float32) + rng.uniform(0, 1e-3, (500, 3, 3)).astype(np.float32)
-    for pos in (one, np.repeat(one, 50, axis=0), np.concatenate([tiny, np.repeat(one, 7, axis=0)])):
+    # 100,000 identical triangles: every clustering distance ties, which the
+    # pair order turns into (2k, 2k + 1) merges -- a balanced tree in
+    # ~17 iterations, not one merge per iteration
+    for pos in (one, np.repeat(one, 50, axis=0), np.concatenate([tiny, np.repeat(one, 7, axis=0)]),
+                np.repeat(one, 100000, axis=0)):
         sc = scenes.cornell_box()
         # the Cornell box keeps its light and camera; the test geometry replaces its first faces
         n = len(pos)
@@ -61,3 +65,4 @@ def test_gpu_tree_degenerate_inputs(cuda):
         g = GB300Scene(sc2, builder="gpu")
         nodes, tris = g.export_bvh()
         check_tree(p, nodes, tris, g.info.max_depth)
+        assert g.info.max_depth <= 12
