@@ -131,6 +131,8 @@ SIGNATURES = {
     "crt_bvh_build_host": (C.c_int, [P, U32, U32, P, P, P, P]),
     "crt_scene_set_bvh_width": (C.c_int, [P, U32]),
     "crt_scene_set_materials": (C.c_int, [P, P, U32]),
+    "crt_scene_set_visit_limit": (C.c_int, [P, U32]),
+    "crt_scene_clear_errors": (C.c_int, [P]),
     "crt_trace_closest": (C.c_int, [P, P, U32, P, P, P, P]),
     "crt_trace_counts": (C.c_int, [P, P, U32, P, P, P]),
     "crt_render_options_default": (None, [P]),

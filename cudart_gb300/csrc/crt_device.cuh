@@ -29,7 +29,7 @@ enum Bsdf : int { DIFFUSE = 0, SPECULAR = 1, DIFFSPEC = 2, MICROFACET = 3, REFRA
 constexpr int kStackShared = 16;
 constexpr int kStackSharedMax = 32;
 constexpr int kMaxLevels = 64;
-constexpr uint32_t kMaxNodeVisits = 1u << 20;   // watchdog per traversal
+constexpr uint32_t kMaxNodeVisits = 1u << 20;   // default watchdog per traversal
 
 enum ErrorBits : uint32_t { ERR_WATCHDOG = 1u, ERR_STACK = 2u };
 
@@ -51,7 +51,8 @@ struct DevScene {
     uint32_t n_lights;
     float lights_area;
     uint32_t n_faces;
-    uint32_t* error;           // ErrorBits, sticky
+    uint32_t max_visits;       // node visits a traversal may make (watchdog)
+    uint32_t* error;           // ErrorBits, sticky until crt_scene_clear_errors
 };
 
 struct Camera {
@@ -415,7 +416,7 @@ struct Traversal {
             if (st.sp >= kMaxLevels) { atomicOr(S.error, ERR_STACK); return true; }
             st.push(make_uint2(grp.x, (hits << 8) | imask));
         }
-        if (++visits > kMaxNodeVisits) { atomicOr(S.error, ERR_WATCHDOG); return true; }
+        if (++visits > S.max_visits) { atomicOr(S.error, ERR_WATCHDOG); return true; }
         if (COUNT) stats->nodes++;
 
         uint32_t child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask;

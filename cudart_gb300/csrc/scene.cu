@@ -436,6 +436,7 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
     D.n_lights = (uint32_t)s->lights.size();
     D.lights_area = lights_area;
     D.n_faces = n;
+    D.max_visits = kMaxNodeVisits;
     D.error = s->error.as<uint32_t>();
 
     crt_scene_info& I = s->info;
@@ -453,6 +454,21 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
 
 int crt_scene_destroy(crt_scene s) {
     delete s;
+    return CRT_OK;
+}
+
+int crt_scene_set_visit_limit(crt_scene s, uint32_t max_visits) {
+    if (!s) return set_error(CRT_ERR_INVALID, "crt_scene_set_visit_limit: null scene");
+    CRT_CUDA(cudaDeviceSynchronize());   // passes already queued keep their limit
+    s->dev.max_visits = max_visits ? max_visits : kMaxNodeVisits;
+    ++s->generation;   // render handles re-capture their wave graphs with it
+    return CRT_OK;
+}
+
+int crt_scene_clear_errors(crt_scene s) {
+    if (!s) return set_error(CRT_ERR_INVALID, "crt_scene_clear_errors: null scene");
+    CRT_CUDA(cudaDeviceSynchronize());
+    CRT_CUDA(cudaMemset(s->error.p, 0, 16));
     return CRT_OK;
 }
 

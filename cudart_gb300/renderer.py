@@ -175,6 +175,14 @@ class GB300Scene:
         mats = _material_table(self.arrays.materials, kd, ka)
         check(load().crt_scene_set_materials(self.handle, mats, len(mats)))
 
+    def set_visit_limit(self, max_visits: int) -> None:
+        """Node visits a traversal may make before the watchdog ends it (0 = default)."""
+        check(load().crt_scene_set_visit_limit(self.handle, max_visits))
+
+    def clear_errors(self) -> None:
+        """Reset the scene's sticky device error word (after CRT_ERR_WATCHDOG)."""
+        check(load().crt_scene_clear_errors(self.handle))
+
     def set_bvh_width(self, width: int) -> None:
         """Rebuild the BVH with 4 or 8 children per node (same geometry)."""
         check(load().crt_scene_set_bvh_width(self.handle, width))

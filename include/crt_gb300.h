@@ -197,6 +197,16 @@ CRT_EXPORT int crt_scene_export_bvh(crt_scene scene, void* nodes, void* triangle
  * first, so passes already queued finish with the old table.
  * No reference counterpart (the optimisation loop of the adjoint). */
 CRT_EXPORT int crt_scene_set_materials(crt_scene scene, const crt_material* materials, uint32_t n);
+/* Failure detection.  Every traversal counts the nodes it visits; past the
+ * limit (default 2^20, 0 restores it) the ray ends as a miss and the scene's
+ * device error word records it, so that the next crt_render_resolve /
+ * _accum / _synchronize returns CRT_ERR_WATCHDOG (as it does for a traversal
+ * stack overflow) instead of a GPU hang.  The error word stays set until
+ * crt_scene_clear_errors.  Both wait for the device to go idle first; the
+ * limit applies to passes started afterwards.  No reference counterpart
+ * (the reference's traversal has no bound, renderer.cu:283-330). */
+CRT_EXPORT int crt_scene_set_visit_limit(crt_scene scene, uint32_t max_visits);
+CRT_EXPORT int crt_scene_clear_errors(crt_scene scene);
 /* Rebuilds the scene's BVH with 4 or 8 children per node from its own
  * triangle records (the geometry is unchanged, so every query answers the
  * same) and uploads it in place of the current one; the autotuner's BVH
