@@ -30,6 +30,7 @@ constexpr int kStackShared = 16;
 constexpr int kStackSharedMax = 32;
 constexpr int kMaxLevels = 64;
 constexpr uint32_t kMaxNodeVisits = 1u << 20;   // default watchdog per traversal
+constexpr uint32_t kVisitCeiling = 1u << 30;    // largest limit; the counter starts at ceiling - limit
 
 enum ErrorBits : uint32_t { ERR_WATCHDOG = 1u, ERR_STACK = 2u };
 
@@ -51,7 +52,7 @@ struct DevScene {
     uint32_t n_lights;
     float lights_area;
     uint32_t n_faces;
-    uint32_t max_visits;       // node visits a traversal may make (watchdog)
+    uint32_t max_visits;       // node visits a traversal may make (watchdog), <= kVisitCeiling
     uint32_t* error;           // ErrorBits, sticky until crt_scene_clear_errors
 };
 
@@ -250,7 +251,11 @@ struct Traversal {
     bool occluded;
     Hit h;
 
-    CRT_D void init(float3 o_, float3 d_, float tmin_, float tmax, int32_t target_, Stack& st) {
+    // max_visits: the scene's watchdog limit (DevScene::max_visits); the
+    // counter starts at kVisitCeiling - max_visits so that every visit
+    // compares against a constant.
+    CRT_D void init(float3 o_, float3 d_, float tmin_, float tmax, int32_t target_, Stack& st,
+                    uint32_t max_visits) {
         o = o_;
         d = d_;
         ix = safe_rcp(d.x);
@@ -260,7 +265,7 @@ struct Traversal {
         oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
         grp = make_uint2(0u, ((1u << oct) << 8) | 1u);   // root = slot 0 of a virtual parent
         tri_base = tri_mask = 0;
-        visits = 0;
+        visits = kVisitCeiling - max_visits;
         target = target_;
         occluded = false;
         h.t = tmax;
@@ -416,7 +421,7 @@ struct Traversal {
             if (st.sp >= kMaxLevels) { atomicOr(S.error, ERR_STACK); return true; }
             st.push(make_uint2(grp.x, (hits << 8) | imask));
         }
-        if (++visits > S.max_visits) { atomicOr(S.error, ERR_WATCHDOG); return true; }
+        if (++visits > kVisitCeiling) { atomicOr(S.error, ERR_WATCHDOG); return true; }
         if (COUNT) stats->nodes++;
 
         uint32_t child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask;
@@ -444,7 +449,7 @@ template <bool OCCLUDED, bool COUNT, bool F32 = false>
 CRT_D bool traverse(const DevScene& S, float3 o, float3 d, float tmin, Hit& h, int32_t target,
                     Stack& st, TraversalStats* stats) {
     Traversal<OCCLUDED, COUNT, true, F32> T;
-    T.init(o, d, tmin, h.t, target, st);
+    T.init(o, d, tmin, h.t, target, st, S.max_visits);
     while (!T.step(S, st, stats)) {
     }
     if (!OCCLUDED) h = T.h;

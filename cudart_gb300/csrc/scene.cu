@@ -460,6 +460,7 @@ int crt_scene_destroy(crt_scene s) {
 int crt_scene_set_visit_limit(crt_scene s, uint32_t max_visits) {
     if (!s) return set_error(CRT_ERR_INVALID, "crt_scene_set_visit_limit: null scene");
     CRT_CUDA(cudaDeviceSynchronize());   // passes already queued keep their limit
+    if (max_visits > kVisitCeiling) return set_error(CRT_ERR_LIMIT, "crt_scene_set_visit_limit: at most 2^30 visits");
     s->dev.max_visits = max_visits ? max_visits : kMaxNodeVisits;
     ++s->generation;   // render handles re-capture their wave graphs with it
     return CRT_OK;

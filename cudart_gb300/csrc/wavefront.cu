@@ -399,7 +399,7 @@ struct ExtendJob {
     CRT_D ExtendJob(const WaveParams& W_, QueueView q_, Stack& st_) : W(W_), q(q_), st(st_) {}
     CRT_D void start(uint32_t i) {
         path = q.at(i);
-        T.init(xyz(W.st_o[path]), xyz(W.st_d[path]), kEps, FLT_MAX, -1, st);
+        T.init(xyz(W.st_o[path]), xyz(W.st_d[path]), kEps, FLT_MAX, -1, st, W.R.S.max_visits);
     }
     CRT_D bool step() { return T.step(W.R.S, st, nullptr); }
     CRT_D void finish() {
@@ -535,7 +535,7 @@ struct ShadowJob {
         entry = i;
         const float4* e = W.shadow + 3ull * i;
         const float4 b = e[1];
-        T.init(xyz(e[0]), xyz(b), kEps, b.w, (int32_t)__float_as_uint(e[2].w), st);
+        T.init(xyz(e[0]), xyz(b), kEps, b.w, (int32_t)__float_as_uint(e[2].w), st, W.R.S.max_visits);
     }
     CRT_D bool step() { return T.step(W.R.S, st, nullptr); }
     // a visible light adds the request's contribution to the path colour
