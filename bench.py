@@ -205,7 +205,8 @@ def adjoint_leg(args, torch, stream):
     adjoint/forward: one adjoint pass (primal trace + replay, both on the GPU)
     against one forward wavefront pass of the same 64 spp (CUDA events, median
     of 5).  Then the material inversion: target 1024 spp with the true
-    albedos, start at albedo 0.5 for the 32 boxes, L2 image loss, Adam at
+    albedos, start at albedo 0.5 for the 32 boxes, L2 loss on the image
+    clamped to [0, 1] (the displayed range), Adam at
     lr 1e-2 for `inversion_iters` iterations, gradients from the adjoint on
     samples independent of the iteration's image (the same samples would
     correlate the residual with its derivative and bias the gradient)."""
@@ -262,7 +263,8 @@ def adjoint_leg(args, torch, stream):
         g.set_materials(kd=kd_vals)
         r.restart(1 << 25)   # not the target's samples (1 << 24) nor the iterations'
         r.render(1024)
-        return float(((torch.from_numpy(r.accum()).cuda() / 1024 - target) ** 2).sum())
+        img = torch.from_numpy(r.accum()).cuda() / 1024
+        return float(((img.clamp(0, 1) - target.clamp(0, 1)) ** 2).sum())
 
     clean0 = image_loss(kd)
     losses = []
@@ -272,10 +274,13 @@ def adjoint_leg(args, torch, stream):
         r.restart(it * sc.spp)
         r.render(sc.spp)
         img = torch.from_numpy(r.accum()).cuda() / sc.spp
-        diff = img - target
+        # L2 on display-range radiance (clamped to [0, 1], as the RGBA8 output
+        # quantises it): the unbounded HDR loss is dominated by a few
+        # fireflies near the lights
+        diff = img.clamp(0, 1) - target.clamp(0, 1)
         loss = float((diff ** 2).sum())
         losses.append(loss)
-        adj[:, :3] = 2.0 * diff / sc.spp
+        adj[:, :3] = 2.0 * diff * (img < 1).float() / sc.spp
         gkd.zero_()
         gka.zero_()
         r.adjoint((1 << 23) + it * sc.spp, sc.spp, adj.data_ptr(), gkd.data_ptr(), gka.data_ptr())
@@ -301,8 +306,8 @@ def adjoint_leg(args, torch, stream):
                         "albedo_rmse_start": round(err0, 4),
                         "albedo_rmse_end": round(float(np.sqrt(np.mean((kd[boxes] - kd_true[boxes]) ** 2))), 4),
                         "seconds": seconds,
-                        "note": "loss_first / loss_last are single 64-spp iterations (Monte Carlo noise "
-                                "dominates them); the medians and the 1024-spp image losses show the trend"}
+                        "note": "loss_first / loss_last are single noisy 64-spp iterations; the medians and "
+                                "the 1024-spp image losses (own samples) are the noise-robust measures"}
     return out
 
 
