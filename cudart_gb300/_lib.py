@@ -116,6 +116,7 @@ SCENE_KA_SCALED = 2
 FLAG_LANE_REFILL = 1
 FLAG_SPLIT_LEAF = 2
 FLAG_OCTANT_QUEUES = 4
+FLAG_SERIAL_SHADOW = 8
 
 
 # name -> (restype, argtypes); every entry point of include/crt_gb300.h

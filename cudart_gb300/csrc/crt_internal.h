@@ -160,6 +160,9 @@ inline int check_render_options(const crt_render_options& o) {
         return set_error(CRT_ERR_INVALID, "queue_chunk must be 0, 32, 64, 128 or 256");
     if (o.top_nodes > 128) return set_error(CRT_ERR_INVALID, "top_nodes must be in [0, 128]");
     if (o.refill_busy > 31) return set_error(CRT_ERR_INVALID, "refill_busy must be in [0, 31]");
+    if (o.flags & ~(uint32_t)(CRT_FLAG_LANE_REFILL | CRT_FLAG_SPLIT_LEAF | CRT_FLAG_OCTANT_QUEUES |
+                              CRT_FLAG_SERIAL_SHADOW))
+        return set_error(CRT_ERR_INVALID, "unknown render flag");
     return CRT_OK;
 }
 

@@ -628,6 +628,29 @@ __global__ void wf_flip(WaveParams W) {
     W.counters[C_FETCH_SHD] = 0;
 }
 
+// wf_flip in two halves, for waves whose shadow traversal of bounce b runs
+// beside the extension traversal of bounce b + 1: the extension queues
+// switch before extend(b + 1), the shadow counters reset after shadow(b).
+__global__ void wf_flip_ext(WaveParams W) {
+    const uint32_t cur = W.counters[C_CUR];
+    W.counters[cur] = 0;
+    if (W.octant) {
+        uint32_t total = 0;
+        for (int k = 0; k < 8; ++k) {
+            W.counters[(cur ? C_OCT1 : C_OCT0) + k] = 0;
+            total += W.counters[(cur ? C_OCT0 : C_OCT1) + k];
+        }
+        W.counters[cur ^ 1u] = total;
+    }
+    W.counters[C_CUR] = cur ^ 1u;
+    W.counters[C_FETCH_EXT] = 0;
+}
+
+__global__ void wf_flip_shadow(WaveParams W) {
+    W.counters[C_SHADOW] = 0;
+    W.counters[C_FETCH_SHD] = 0;
+}
+
 __global__ void __launch_bounds__(256) wf_accumulate(WaveParams W) {
     const uint4 wd = wave_desc(W);
     const WaveSeg* segs = W.segs + wd.x;
@@ -896,13 +919,39 @@ static WaveGrids wave_grids(crt_render r, uint32_t capacity) {
 // Enqueue the body of one wave (generation and every bounce); captured into
 // a wave set's graph.  The accumulate and wave-advance kernels follow it
 // outside the graph so that accumulates of concurrent sets can be ordered.
-static void enqueue_wave_body(const WaveParams& W, const WaveGrids& G, uint32_t max_depth, cudaStream_t s) {
+//
+// With `s2` (and two events), bounce b's shadow traversal is a branch of its
+// own: it starts after shade(b) and runs beside the queue switch and
+// extend(b + 1); shade(b + 1) -- which appends new shadow requests and reads
+// the path colours shadow(b) adds to -- waits for it.  The two traversals
+// touch disjoint state (hit records vs colours and the shadow queue), and
+// as persistent kernels each fills the tail of the other.
+static void enqueue_wave_body(const WaveParams& W, const WaveGrids& G, uint32_t max_depth, cudaStream_t s,
+                              cudaStream_t s2 = nullptr, cudaEvent_t shaded = nullptr,
+                              cudaEvent_t shadowed = nullptr) {
     wf_generate<false><<<G.gen, kWaveBlock, 0, s>>>(W);
     for (uint32_t b = 0; b < max_depth; ++b) {
         G.extend<<<G.ext, G.tblock, G.tsmem, s>>>(W);
+        if (!s2) {
+            wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
+            G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W);
+            wf_flip<<<1, 1, 0, s>>>(W);
+            continue;
+        }
+        if (b > 0) {
+            cudaStreamWaitEvent(s, shadowed, 0);   // shadow(b - 1) is done
+            wf_flip_shadow<<<1, 1, 0, s>>>(W);
+        }
         wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
-        G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W);
-        wf_flip<<<1, 1, 0, s>>>(W);
+        cudaEventRecord(shaded, s);
+        cudaStreamWaitEvent(s2, shaded, 0);
+        G.shadow<<<G.shd, G.tblock, G.tsmem, s2>>>(W);
+        cudaEventRecord(shadowed, s2);
+        wf_flip_ext<<<1, 1, 0, s>>>(W);
+    }
+    if (s2) {
+        cudaStreamWaitEvent(s, shadowed, 0);   // the branch rejoins before the wave ends
+        wf_flip_shadow<<<1, 1, 0, s>>>(W);
     }
 }
 
@@ -1004,14 +1053,26 @@ static int capture_set_graph(crt_render r, WaveSet& set) {
     const WaveParams W = wave_params(r, set);
     const WaveGrids G = wave_grids(r, set.buf.capacity);
     CRT_CUDA(cudaGetLastError());
-    // Captured on a private stream; launched on the set's stream.
-    cudaStream_t cap = nullptr;
+    // Captured on a private stream (and a second one for the shadow
+    // branches); launched on the set's stream.
+    const bool overlap = (r->opts.flags & CRT_FLAG_SERIAL_SHADOW) == 0;
+    cudaStream_t cap = nullptr, cap2 = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
     CRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaSuccess;
+    if (overlap) {
+        e = cudaStreamCreateWithFlags(&cap2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        enqueue_wave_body(W, G, r->opts.max_depth, cap);
+        enqueue_wave_body(W, G, r->opts.max_depth, cap, cap2, ev[0], ev[1]);
         e = cudaStreamEndCapture(cap, &g->graph);
     }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    if (cap2) cudaStreamDestroy(cap2);
     cudaStreamDestroy(cap);
     if (e != cudaSuccess) return cuda_error(e, "capture wave graph");
     CRT_CUDA(cudaGraphInstantiate(&g->exec, g->graph, 0));

@@ -252,12 +252,16 @@ enum {
                                    at once (warp-local pool of queue entries) */
     CRT_FLAG_SPLIT_LEAF = 2u,   /* one triangle test per traversal step, so lanes
                                    in leaves and lanes in inner nodes interleave */
-    CRT_FLAG_OCTANT_QUEUES = 4u /* shade files surviving paths by the octant of
+    CRT_FLAG_OCTANT_QUEUES = 4u, /* shade files surviving paths by the octant of
                                    their next direction (8 queue regions, each in
                                    path order), so a warp of the extend kernel
                                    mostly holds rays of one octant: the same child
                                    order at every node.  8x the queue memory; not
                                    used by crt_render_tile_noalloc */
+    CRT_FLAG_SERIAL_SHADOW = 8u /* trace each bounce's shadow rays before the next
+                                   bounce's extension rays.  By default the two
+                                   (independent) traversals are branches of the
+                                   wave graph and fill each other's tails */
 };
 
 typedef struct {
