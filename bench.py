@@ -503,9 +503,13 @@ def run_gb300(args):
                    "kind": "port",
                    "sample": (f"{len(px)} stratified pixels x 1 spp" if px is not None
                               else f"full frame x {k_spp} spp") + f" of the 1920x1080 frame, {dt:.1f} s"}
-        cap = wf.options.wave_paths or (1 << 22)
+        cap = wf.options.wave_paths or default_wave_paths(npix)
         waves = math.ceil(spp / max(1, cap // npix)) if npix <= cap else spp * math.ceil(npix / cap)
-        launches = args.steps * waves * (3 + 4 * sc.max_depth)
+        # per wave: generate, accumulate, next-wave; per bounce: extend, shade,
+        # shadow and the queue switch, plus the shadow-counter reset of the
+        # overlapped schedule (once per bounce; the serial one folds it in)
+        serial = bool(wf.options.flags & 8)
+        launches = args.steps * waves * (3 + (4 if serial else 5) * sc.max_depth)
         out = {
             "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
@@ -531,6 +535,15 @@ def run_gb300(args):
         dist.destroy_process_group()
     if out is not None:
         print(json.dumps(out), flush=True)
+
+
+def default_wave_paths(pixels: int) -> int:
+    """The library's default paths per wave set (default_wave_paths in
+    cudart_gb300/csrc/crt_internal.h)."""
+    cap = 1 << 16
+    while cap < pixels * 8 and cap < (1 << 24):
+        cap <<= 1
+    return cap
 
 
 def run_build_only(args) -> None:

