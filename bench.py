@@ -441,6 +441,11 @@ def run_gb300(args):
                     "peak": peak, "unit": "GB/s", "frac": round(main["gbs"] / peak, 4),
                     "traffic": traffic, "peak_kind": f"{peak_kind} (HBM copy)",
                     "algorithmic_bytes": f"nodes visited x {node_bytes} B + triangles tested x 48 B per ray",
+                    "dram_share_of_algorithmic": (round(traffic / main["bytes_per_launch"], 4)
+                                                  if traffic else None),
+                    "reading": "achieved counts the node and triangle bytes the traversal consumes; most are "
+                               "L1/L2 hits (traffic is the DRAM part), so frac can exceed 1: the kernel is "
+                               "issue/latency-bound, not HBM-bound",
                     "stage_ms": {s: round(prof[f"{s}_ms"], 2) for s in stages},
                     "profile_spp": 8,
                     "extend_rays_by_bounce": prof["extend_rays_by_bounce"][:sc.max_depth],
