@@ -344,7 +344,7 @@ def run_gb300(args):
     tuned = None
     if not args.no_tune:
         t0 = time.perf_counter()
-        tune = autotune(scene, sc.width, sc.height, max_depth=sc.max_depth, trial_spp=8, repeats=2,
+        tune = autotune(scene, sc.width, sc.height, max_depth=sc.max_depth, trial_spp=32, repeats=2,
                         rounds=1, tune_bvh_width=False)
         tuned = {"options": {k: v for k, v in options_dict(tune.options).items()
                              if k not in ("seed", "max_depth", "view_id")},
