@@ -171,7 +171,7 @@ def batched_views_leg(args, torch, stream):
     samples = sum(v.width * v.height * v.spp for v in views)
     g = GB300Scene(sc)
     t0 = time.perf_counter()
-    tune = autotune(g, 1024, 1024, max_depth=sc.max_depth, trial_spp=4, repeats=2, rounds=1,
+    tune = autotune(g, 1024, 1024, max_depth=sc.max_depth, trial_spp=16, repeats=2, rounds=1,
                     tune_bvh_width=True)
     tune_s = time.perf_counter() - t0
     opts = tune.options
