@@ -141,8 +141,12 @@ class GB300Scene:
             mats = _material_table(sc.materials)
         dims = np.asarray([d for img in sc.textures for d in (img.shape[1], img.shape[0])], np.uint32)
         # RGBA8 texels, converted on the device as stbi_loadf converts them
-        rgba = (np.concatenate([_rgba8(img) for img in sc.textures]) if sc.textures
-                else np.zeros(4, np.uint8))
+        if len(sc.textures) == 1:
+            rgba = _rgba8(sc.textures[0])          # a view: no copy of the caller's (maybe pinned) bytes
+        elif sc.textures:
+            rgba = np.concatenate([_rgba8(img) for img in sc.textures])
+        else:
+            rgba = np.zeros(4, np.uint8)
         li = (np.ascontiguousarray(lights, np.uint32) if lights is not None
               else np.zeros(1, np.uint32))
         self._keep += [pos, nor, uvs, mid, mats, dims, rgba, li]
@@ -284,8 +288,12 @@ class GB300Renderer:
     def render(self, n_spp: Optional[int] = None) -> None:
         check(load().crt_render_pass(self.handle, self.samples if n_spp is None else n_spp))
 
-    def copy_image_bytes(self) -> np.ndarray:
-        out = np.zeros((self.height, self.width, 4), np.uint8)
+    def copy_image_bytes(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """RGBA8 [h, w, 4] (crt_render_resolve); `out` (e.g. pinned) is filled if given."""
+        if out is None:
+            out = np.zeros((self.height, self.width, 4), np.uint8)
+        elif out.shape != (self.height, self.width, 4) or out.dtype != np.uint8 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous uint8 [height, width, 4] array")
         check(load().crt_render_resolve(self.handle, _ptr(out)))
         return out
 
