@@ -251,6 +251,16 @@ def cornell_box(width=512, height=512, spp=16, max_depth=5) -> SceneArrays:
     return _finish(mb, mats, [], CORNELL_CAMERA, width, height, spp, max_depth)
 
 
+def cornell_lens(width=96, height=96, spp=16, max_depth=6) -> SceneArrays:
+    """The Cornell box through a thin lens: aperture focalLength / fStop =
+    0.5 / 4 = 0.125, focused at |viewDirection| = 3.9 (the box centre), so
+    the camera's lens-jitter path (camera.cu:38-57) is exercised."""
+    sc = cornell_box(width, height, spp, max_depth)
+    cam = CameraSpec(CORNELL_CAMERA.fov_deg, CORNELL_CAMERA.eye, (0.0, 0.0, -3.9), CORNELL_CAMERA.up,
+                     focal_length=0.5, fstop=4.0)
+    return dataclasses.replace(sc, camera=cam)
+
+
 def mixed_mid(seed=2, width=1280, height=720, spp=128, max_depth=8, subdiv=5) -> SceneArrays:
     """Cornell shell + 5 icospheres (radial noise +-2%); seeded materials:
     diffuse U(0.1,0.9), mirror, or glass with IOR 1.5."""

@@ -46,6 +46,7 @@ def _configs():
         "cornell_512": (lambda: scenes.cornell_box(), 4096, 0.95, 256, 4096, "crop+random"),
         "feature_mix": (lambda: scenes.feature_mix(), 4096, 0.95, 512, 1024, "all"),
         "mixed_sub2": (lambda: scenes.mixed_mid(width=64, height=48, subdiv=2), 4096, 0.95, 0, 0, None),
+        "cornell_lens": (lambda: scenes.cornell_lens(), 1024, 0.95, 256, 2048, "crop+random"),
     }
 
 

@@ -44,7 +44,7 @@ def _gpu_means(sc, fx, seed, mode):
     return acc.astype(np.float64) / spp, acc
 
 
-@pytest.mark.parametrize("name", ["cornell_512", "feature_mix"])
+@pytest.mark.parametrize("name", ["cornell_512", "feature_mix", "cornell_lens"])
 @pytest.mark.parametrize("mode", ["megakernel", "wavefront"])
 def test_same_stream_relative_mse(cuda, name, mode):
     fx, sc = _fixture(name)
@@ -58,7 +58,7 @@ def test_same_stream_relative_mse(cuda, name, mode):
     assert np.all(rel <= 1e-6), rel
 
 
-@pytest.mark.parametrize("name", ["cornell_512", "feature_mix"])
+@pytest.mark.parametrize("name", ["cornell_512", "feature_mix", "cornell_lens"])
 def test_independent_stream_z_test(cuda, name):
     fx, sc = _fixture(name)
     n = int(fx["stats_spp"])

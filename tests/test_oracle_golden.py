@@ -15,7 +15,7 @@ import oracle
 from conftest import GOLDEN
 from golden.make_golden import load_scene
 
-FIXTURES = ["cornell_512", "feature_mix", "mixed_sub2"]
+FIXTURES = ["cornell_512", "feature_mix", "mixed_sub2", "cornell_lens"]
 
 
 def _fx(name):
@@ -89,7 +89,7 @@ def test_closest_hit_matches_reference(name):
     assert np.array_equal(buv[hit], fx["ref_hit_uv"][hit])
 
 
-@pytest.mark.parametrize("name", ["cornell_512", "feature_mix"])
+@pytest.mark.parametrize("name", ["cornell_512", "feature_mix", "cornell_lens"])
 def test_samples_match_reference(name):
     fx = _fx(name)
     o = oracle.scene_from_export(_export(fx))
@@ -101,7 +101,7 @@ def test_samples_match_reference(name):
         assert np.array_equal(acc[0], rgb), (x, y, s)
 
 
-@pytest.mark.parametrize("name", ["cornell_512", "feature_mix"])
+@pytest.mark.parametrize("name", ["cornell_512", "feature_mix", "cornell_lens"])
 def test_long_render_statistics_match_reference(name):
     fx = _fx(name)
     o = oracle.scene_from_export(_export(fx))
