@@ -53,3 +53,13 @@ def test_ray_queries_keep_working_after_a_watchdog(cuda):
     g.clear_errors()
     idx1, t1, _ = g.trace_closest(rays)
     assert torch.equal(idx0, idx1) and torch.equal(t0, t1)
+
+
+def test_visit_limit_range(cuda):
+    from cudart_gb300 import load
+    g = GB300Scene(scenes.cornell_box(width=16, height=16))
+    L = load()
+    assert L.crt_scene_set_visit_limit(g.handle, (1 << 30) + 1) == 6     # CRT_ERR_LIMIT
+    assert L.crt_scene_set_visit_limit(g.handle, 1 << 30) == 0
+    assert L.crt_scene_set_visit_limit(None, 5) == 1
+    assert L.crt_scene_clear_errors(None) == 1

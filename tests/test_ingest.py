@@ -390,3 +390,34 @@ def test_texel_table_pins_every_byte_value():
     assert (w, h) == (16, 16)
     assert np.array_equal(tex, LUT[img])
     assert len(np.unique(img[:, 0])) == 256
+
+
+# ---------------------------------------------------------------------------
+# C ABI argument checks (no GPU)
+# ---------------------------------------------------------------------------
+def test_c_abi_argument_errors(tmp_path):
+    from cudart_gb300 import load
+    L = load()
+    h = C.c_void_p()
+    assert L.crt_scene_files_load(None, None, 0, C.byref(h)) == 1
+    assert L.crt_scene_files_load(b"x.obj", None, 0, None) == 1
+    obj = _write(tmp_path, "mtllib s.mtl\nusemtl m\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    assert L.crt_scene_files_load(obj.encode(), None, 0x100, C.byref(h)) == 1      # unknown flag
+    assert "unknown flags" in L.crt_last_error().decode()
+    assert L.crt_scene_files_load(obj.encode(), None, 0, C.byref(h)) == 0
+    assert L.crt_scene_files_desc(h, None) == 1
+    assert L.crt_scene_files_get_info(None, None) == 1
+    assert L.crt_scene_files_mesh(h, 99, None, None, None) == 1
+    assert L.crt_scene_files_destroy(h) == 0
+    assert L.crt_camera_load_json(None, 1, 1, None) == 1
+    dims = (C.c_uint32 * 2)()
+    png = tmp_path / "t.png"
+    png.write_bytes(png_bytes(np.zeros((4, 5, 3), np.uint8), 2))
+    assert L.crt_texture_load_png(str(png).encode(), dims, None, 0) == 0 and tuple(dims) == (5, 4)
+    buf = np.zeros(3 * 20, np.float32)
+    assert L.crt_texture_load_png(str(png).encode(), dims, buf.ctypes.data, 19) == 1   # too small
+    assert L.crt_texture_load_png(str(png).encode(), dims, buf.ctypes.data, 20) == 0
+    img = np.zeros((2, 2, 4), np.uint8)
+    assert L.crt_image_write_png(str(tmp_path / "o.png").encode(), 0, 2, img.ctypes.data) == 1
+    assert L.crt_image_write_png(str(tmp_path / "o.png").encode(), 1 << 20, 1 << 12, img.ctypes.data) == 6
+    assert L.crt_image_write_png(str(tmp_path / "no" / "dir" / "o.png").encode(), 2, 2, img.ctypes.data) == 1
