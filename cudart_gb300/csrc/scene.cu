@@ -145,20 +145,26 @@ inline float bits(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
 // Scene::loadTriangles (scene.cpp:111-130): v1, e1 = v2 - v1, e2 = v3 - v1
 // (or the edges as given), area = |e1 x e2| / 2; shading records (three
 // normals, area, material id) and uvs.
+// A face with a non-finite coordinate sets *bad (the builds bin by centroid
+// and must not see NaN or infinity).
 __global__ void k_pack_faces(const float* __restrict__ pos, const float* __restrict__ nor,
                              const float* __restrict__ uv, const uint32_t* __restrict__ mid, uint32_t n, bool edges,
                              float* __restrict__ v1, float* __restrict__ e1, float* __restrict__ e2,
-                             float4* __restrict__ shade, float4* __restrict__ uvs) {
+                             float4* __restrict__ shade, float4* __restrict__ uvs, uint32_t* bad) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float* p = pos + 9ull * i;
         float a[3], b[3];
+        bool finite = true;
         for (int k = 0; k < 3; ++k) {
             a[k] = edges ? p[3 + k] : p[3 + k] - p[k];
             b[k] = edges ? p[6 + k] : p[6 + k] - p[k];
+            finite = finite && isfinite(p[k]) && isfinite(p[k] + a[k]) && isfinite(p[k] + b[k]) &&
+                     isfinite(a[k]) && isfinite(b[k]);
             v1[3ull * i + k] = p[k];
             e1[3ull * i + k] = a[k];
             e2[3ull * i + k] = b[k];
         }
+        if (!finite) atomicMin(bad, i);
         const float cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
         const float area = sqrtf(cx * cx + cy * cy + cz * cz) / 2.0f;
         const float* nn = nor + 9ull * i;
@@ -364,7 +370,10 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
             delete s;
             return st;
         }
-        cudaError_t e = dv1.alloc(12ull * n);
+        DevBuf dbad;
+        cudaError_t e = dbad.alloc(4);
+        if (e == cudaSuccess) e = cudaMemset(dbad.p, 0xFF, 4);   // lowest bad face, or UINT32_MAX
+        if (e == cudaSuccess) e = dv1.alloc(12ull * n);
         if (e == cudaSuccess) e = de1.alloc(12ull * n);
         if (e == cudaSuccess) e = de2.alloc(12ull * n);
         if (e == cudaSuccess) e = s->shade.alloc(48ull * n);
@@ -373,9 +382,16 @@ int crt_scene_create(const crt_scene_desc* d, crt_scene* out) {
         const uint32_t grid = (uint32_t)std::min<uint64_t>((n + 255) / 256, 4096);
         k_pack_faces<<<grid, 256>>>(dpos.as<float>(), dnor.as<float>(), d->uvs ? duv.as<float>() : nullptr,
                                     dmid.as<uint32_t>(), n, (d->flags & CRT_SCENE_EDGES) != 0, dv1.as<float>(),
-                                    de1.as<float>(), de2.as<float>(), s->shade.as<float4>(), s->uvs.as<float4>());
+                                    de1.as<float>(), de2.as<float>(), s->shade.as<float4>(), s->uvs.as<float4>(),
+                                    dbad.as<uint32_t>());
         e = cudaGetLastError();
+        uint32_t bad_face = UINT32_MAX;
+        if (e == cudaSuccess) e = cudaMemcpy(&bad_face, dbad.p, 4, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) { delete s; return cuda_error(e, "k_pack_faces"); }
+        if (bad_face != UINT32_MAX) {
+            delete s;
+            return set_error(CRT_ERR_INVALID, "non-finite vertex coordinate in face " + std::to_string(bad_face));
+        }
         if (s->builder == CRT_BVH_GPU) {
             st = build_on_device(s, dv1.as<float>(), de1.as<float>(), de2.as<float>(), n, width);
         } else {

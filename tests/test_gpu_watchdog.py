@@ -63,3 +63,16 @@ def test_visit_limit_range(cuda):
     assert L.crt_scene_set_visit_limit(g.handle, 1 << 30) == 0
     assert L.crt_scene_set_visit_limit(None, 5) == 1
     assert L.crt_scene_clear_errors(None) == 1
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+@pytest.mark.parametrize("builder", ["host", "gpu"])
+def test_non_finite_vertices_are_an_error(cuda, bad, builder):
+    import dataclasses
+    sc = scenes.cornell_box(width=16, height=16)
+    pos = sc.positions.copy()
+    pos[7, 1, 2] = bad
+    with pytest.raises(CrtError, match="non-finite vertex coordinate in face 7"):
+        GB300Scene(dataclasses.replace(sc, positions=pos), builder=builder)
+    g = GB300Scene(sc, builder=builder)       # the device is still usable
+    assert g.info.num_triangles == sc.n_tris
