@@ -14,7 +14,7 @@
 // --mode wavefront|megakernel, --depth N (the reference's 6 bounces by
 // default), --seed N, --builder host|gpu, --tune (autotune the wavefront
 // options first), --exact-materials, --env <file>, --json (one JSON line of
-// timings).  --cpu and --x have no counterpart here: this build renders on
+// timings).  --cpu and --x have no counterpart here: this renderer runs on
 // the GPU only and has no window.
 #include <chrono>
 #include <cstdio>
@@ -109,11 +109,11 @@ int run(int argc, char** argv) {
         return 1;
     }
     if (has_flag(args, "--cpu")) {
-        std::cerr << "--cpu: this build has no CPU renderer (it renders on the GPU only)" << std::endl;
+        std::cerr << "--cpu: this renderer has no CPU path (it renders on the GPU only)" << std::endl;
         return 2;
     }
     if (has_flag(args, "--x")) {
-        std::cerr << "--x: this build has no window; the image is written to a PNG file" << std::endl;
+        std::cerr << "--x: this renderer has no window; the image is written to a PNG file" << std::endl;
         return 2;
     }
     std::string env_path = "../.env";

@@ -43,7 +43,7 @@ typedef enum {
     CRT_ERR_INVALID = 1,      /* bad argument or scene description */
     CRT_ERR_CUDA = 2,         /* CUDA runtime error (message has details) */
     CRT_ERR_NOMEM = 3,        /* host or device allocation failed */
-    CRT_ERR_UNSUPPORTED = 4,  /* option not available in this build */
+    CRT_ERR_UNSUPPORTED = 4,  /* option not supported by this library */
     CRT_ERR_WATCHDOG = 5,     /* a device traversal exceeded its step or stack limit */
     CRT_ERR_LIMIT = 6         /* a size exceeds a documented maximum */
 } crt_status;
