@@ -15,6 +15,10 @@ do not depend on size.
   sampled directions, which occasionally send a path elsewhere), so the
   bound is statistical: the relative squared error of the subset sum stays
   below REL_MSE_MAX and at least SAME_MIN of the pixels are bit-exact.
+* The batched-views workload (64 views, 23.2 Mpixels) as one batch equals
+  the 64 views rendered alone, on 8- and 4-wide trees.
+* The material-inversion workload (512x512, depth 6): the adjoint against
+  the oracle's FP64 gradient.
 """
 import os
 
@@ -140,3 +144,63 @@ def test_frame_modes_and_trees_identical(cuda, full):
     print(f"{name}: relative squared error {rel:.3e}, bit-exact pixels {same:.4f}")
     assert rel < REL_MSE_MAX, f"{name}: relative squared error {rel:.3e}"
     assert same > SAME_MIN, f"{name}: only {same:.3f} of pixels bit-exact"
+
+
+def test_batched_views_full_config(cuda):
+    """The 64 views of the batched-views workload over the full mixed scene,
+    at their own resolutions (256^2, 512^2, 768x432, 1024^2), one sample
+    each: the wavefront batch, on 8- and on 4-wide trees, equals every view
+    rendered alone by the plain kernel, bit for bit."""
+    import dataclasses
+
+    from cudart_gb300 import GB300Batch, camera_from_json
+    sc = scenes.mixed_mid()
+    views = [dataclasses.replace(v, spp=1) for v in scenes.batched_views(base=sc).views]
+    assert len(views) == 64
+    g = GB300Scene(sc)
+    singles = []
+    for k, v in enumerate(views):
+        cam = camera_from_json(v.camera, v.width, v.height)
+        r = GB300Renderer(g, v.width, v.height, 1, camera=cam, view_id=k, max_depth=sc.max_depth,
+                          mode="megakernel")
+        r.render()
+        singles.append(r.accum())
+        del r
+    for width in (8, 4):
+        g.set_bvh_width(width)
+        b = GB300Batch(g, views, max_depth=sc.max_depth, mode="wavefront")
+        b.render()
+        b.synchronize()
+        for k in range(len(views)):
+            assert np.array_equal(b.accum(k), singles[k]), f"width {width}, view {k}"
+        del b
+
+
+def test_material_inversion_adjoint_full_size(cuda):
+    """The material-inversion workload at its size (512x512, depth 6, 32
+    box albedos + the light): the path-replay adjoint of 4 samples per pixel
+    against the oracle's FP64 adjoint on the same samples, with the bounds of
+    the small-image adjoint tests."""
+    sc = scenes.material_inversion()
+    assert (sc.width, sc.height, sc.max_depth) == (512, 512, 6)
+    rng = np.random.default_rng(11)
+    adj = rng.uniform(0.5, 1.5, (sc.width * sc.height, 3)).astype(np.float32)
+    g = GB300Scene(sc)
+    r = GB300Renderer(g, sc.width, sc.height, 4, max_depth=sc.max_depth, seed=5, mode="wavefront")
+    a4 = cuda.zeros((adj.shape[0], 4), dtype=cuda.float32, device="cuda")
+    a4[:, :3] = cuda.from_numpy(adj).cuda()
+    n_mats = len(sc.materials)
+    gkd = cuda.zeros((n_mats, 3), dtype=cuda.float32, device="cuda")
+    gka = cuda.zeros((n_mats, 3), dtype=cuda.float32, device="cuda")
+    cuda.cuda.synchronize()
+    r.adjoint(0, 4, a4.data_ptr(), gkd.data_ptr(), gka.data_ptr())
+    r.synchronize()
+    o = oracle.OracleScene(sc)
+    cam = oracle.make_camera(sc.camera, sc.width, sc.height)
+    rkd, rka = o.adjoint(cam, 5, 4, sc.max_depth, adj, threads=os.cpu_count() or 1)
+    for got, ref in ((gkd.cpu().numpy().astype(np.float64), rkd),
+                     (gka.cpu().numpy().astype(np.float64), rka)):
+        sig = np.abs(ref) > 1e-3 * np.abs(ref).max()
+        rel = np.abs(got - ref)[sig] / np.abs(ref)[sig]
+        assert np.median(rel) < 1e-4 and rel.max() < 1e-2, (np.median(rel), rel.max())
+        assert np.all(np.abs(got[~sig]) <= 2e-3 * np.abs(ref).max())
