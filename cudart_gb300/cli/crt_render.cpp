@@ -12,7 +12,8 @@
 //
 // Additions: -o <file> (advertised by the reference, never parsed there),
 // --mode wavefront|megakernel, --depth N (the reference's 6 bounces by
-// default), --seed N, --builder host|gpu, --tune (autotune the wavefront
+// default), --seed N, --builder host|gpu, --nodes f32|q8 (node encoding the
+// render reads; FP32 by default), --tune (autotune the wavefront
 // options first), --exact-materials, --env <file>, --json (one JSON line of
 // timings).  --cpu and --x have no counterpart here: this renderer runs on
 // the GPU only and has no window.
@@ -94,6 +95,7 @@ void usage() {
                  "--depth \t<max bounces>\tdefault: 6\n"
                  "--seed \t<Philox seed>\tdefault: 1234\n"
                  "--builder \t<host|gpu>\tdefault: host\n"
+                 "--nodes \t<f32|q8>\tdefault: f32\n"
                  "--tune \t<autotune the wavefront options first>\n"
                  "--exact-materials \t<one material per MTL entry>\n"
                  "--env \t<.env file>\tdefault: ../.env\n"
@@ -139,11 +141,13 @@ int run(int argc, char** argv) {
     if (flag_value(args, "-o", v)) out_file = v;
     const std::string obj_path = obj_dir + scene_name + ".obj";
     const std::string cam_path = cam_dir + scene_name + "-camera.json";
-    std::string mode = "wavefront", builder = "host";
+    std::string mode = "wavefront", builder = "host", nodes = "f32";
     flag_value(args, "--mode", mode);
     flag_value(args, "--builder", builder);
+    flag_value(args, "--nodes", nodes);
     if (mode != "wavefront" && mode != "megakernel") throw Failure{"--mode must be wavefront or megakernel"};
     if (builder != "host" && builder != "gpu") throw Failure{"--builder must be host or gpu"};
+    if (nodes != "f32" && nodes != "q8") throw Failure{"--nodes must be f32 or q8"};
     if (samples < 1 || width < 1 || height < 1 || depth < 1) throw Failure{"-s, -w, -h and --depth must be positive"};
     const bool json = has_flag(args, "--json");
 
@@ -187,6 +191,7 @@ int run(int argc, char** argv) {
     opts.mode = mode == "wavefront" ? CRT_MODE_WAVEFRONT : CRT_MODE_MEGAKERNEL;
     opts.max_depth = (uint32_t)depth;
     opts.seed = (uint64_t)seed;
+    opts.node_format = nodes == "f32" ? CRT_NODES_F32 : CRT_NODES_Q8;
     if (has_flag(args, "--tune")) {
         if (mode != "wavefront") throw Failure{"--tune applies to the wavefront mode"};
         crt_tune_params params;

@@ -96,6 +96,7 @@ Gb300Renderer::Gb300Renderer(Scene* scene, pixels_t w, pixels_t h, uint spp, boo
     crt_render_options o;
     crt_render_options_default(&o);   // 6 bounces, seed 1234: the reference's values
     o.mode = CRT_MODE_WAVEFRONT;
+    o.node_format = CRT_NODES_F32;    // the faster encoding on the 1080p and mixed scenes
     check(crt_render_create(scene_handle, &c, w, h, &o, &render_handle), "crt_render_create");
     // h_imgPtr comes from the Renderer constructor (renderer.cu:80-85)
     if (cudaMalloc(&d_img, sizeof(uchar4) * (size_t)w * h) != cudaSuccess)

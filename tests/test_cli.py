@@ -52,3 +52,11 @@ def test_bad_camera_is_reported(tmp_path):
                                    f"TEXTURES_PATH={files['textures']}\n")
     p = _run(["-f", "box", "--env", str(tmp_path / ".env")], tmp_path)
     assert p.returncode == 1 and "focalLength" in p.stderr
+
+
+@pytest.mark.parametrize("flag,value,message", [("--nodes", "f16", "--nodes must be f32 or q8"),
+                                                ("--mode", "raster", "--mode must be wavefront or megakernel"),
+                                                ("--builder", "cloud", "--builder must be host or gpu")])
+def test_bad_option_values_are_refused(tmp_path, flag, value, message):
+    p = _run(["-f", "box", flag, value], tmp_path)
+    assert p.returncode == 1 and message in p.stderr
