@@ -168,3 +168,16 @@ def test_textured_mirror_glass(cuda):
     ref, _, _ = _oracle(sc, 8, 8)
     rel = float(np.sum((acc - ref) ** 2) / np.sum(ref ** 2))
     assert rel < 1e-3
+
+
+@pytest.mark.parametrize("size,wave_paths", [((64, 48), 768),     # 3 whole 4-row bands per wave: 8x4 tiles
+                                             ((64, 48), 1000),    # ranges cut mid-band: row order
+                                             ((60, 44), 960),     # width not a multiple of 8: row order
+                                             ((64, 48), 0)])      # whole images per wave: tiles
+def test_pixel_order_within_waves_does_not_change_results(cuda, size, wave_paths):
+    """Waves walk whole 4-row bands in 8x4 pixel tiles and other ranges in
+    row order; every pixel still adds its samples in sample order."""
+    sc = scenes.cornell_box(width=size[0], height=size[1])
+    a = _render(sc, 6, 5, "megakernel").accum()
+    b = _render(sc, 6, 5, "wavefront", wave_paths=wave_paths).accum()
+    assert np.array_equal(a, b)
