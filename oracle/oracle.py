@@ -16,6 +16,18 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liborc.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libcrt_ref.so")
+# The reference with its traversal stack raised to 64 entries and its bounce
+# count set to 8 (oracle/Makefile, target ref-deep): the estimator the depth-8
+# workloads run, on trees deeper than the shipped 16-entry stack allows.
+REF_DEEP_LIB_PATH = os.path.join(HERE, "_ref", "libcrt_ref_s64_d8.so")
+
+
+def reference_root() -> Optional[str]:
+    """The CudaRT project root named by the environment variable CUDART_REF
+    (the reference harness is built only where it is set and holds the
+    sources)."""
+    root = os.environ.get("CUDART_REF", "")
+    return root if root and os.path.isdir(os.path.join(root, "src", "renderer")) else None
 
 TRI_DT = np.dtype([("v1", "<f4", 3), ("e1", "<f4", 3), ("e2", "<f4", 3), ("n1", "<f4", 3),
                    ("n2", "<f4", 3), ("n3", "<f4", 3), ("uv", "<f4", 6), ("area", "<f4"),
@@ -42,8 +54,10 @@ def build(quiet: bool = True) -> None:
     are present on this machine)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-C", HERE, "-s", "all"], stdout=out)
-    if os.path.isdir("/root/reference/src"):
-        subprocess.check_call(["make", "-C", HERE, "-s", "-j8", "ref"], stdout=out)
+    root = reference_root()
+    if root is not None:
+        subprocess.check_call(["make", "-C", HERE, "-s", "-j8", "REF=" + root, "ref", "ref-deep"],
+                              stdout=out)
 
 
 _lib = None
@@ -262,8 +276,10 @@ class RefHarness:
     """The reference's own scene loader, traversal and estimator, loaded
     through oracle/_ref/libcrt_ref.so.  One scene per process."""
 
-    def __init__(self, files: dict, width: int, height: int):
-        L = C.CDLL(REF_LIB_PATH)
+    def __init__(self, files: dict, width: int, height: int, deep: bool = False):
+        """deep: load the ref-deep build (64-entry stack, 8 bounces) instead
+        of the one compiled as shipped (16 entries, 6 bounces)."""
+        L = C.CDLL(REF_DEEP_LIB_PATH if deep else REF_LIB_PATH)
         P = C.c_void_p
         L.ref_load.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int]
         L.ref_counts.argtypes = [P]
@@ -280,6 +296,10 @@ class RefHarness:
                                  P, P, P]
         L.ref_gamma_table.argtypes = [P]
         L.ref_quantise.argtypes = [P, C.c_uint32, C.c_uint32, P]
+        L.ref_limits.argtypes = [P]
+        lim = np.zeros(2, np.uint32)
+        L.ref_limits(_p(lim))
+        self.stack_entries, self.max_depth = int(lim[0]), int(lim[1])
         self.L = L
         n = L.ref_load(files["obj"].encode(), files["camera"].encode(),
                        files["textures"].encode(), width, height)
@@ -291,15 +311,13 @@ class RefHarness:
          self.texels, self.pad) = map(int, c)
         self.width, self.height = width, height
 
-    # intersectBVH keeps `int stack[16]` (renderer.cu:289); a path from the
-    # root longer than 16 nodes overflows it, so traversal calls refuse such
-    # scenes instead of smashing the stack.
-    MAX_TRAVERSAL_DEPTH = 16
-
+    # intersectBVH keeps `int stack[16]` (renderer.cu:289; 64 in the deep
+    # build); a traversal holds at most one entry per level below the root, so
+    # renders refuse trees deeper than the stack instead of smashing it.
     def _check_depth(self):
-        if self.bvh_depth > self.MAX_TRAVERSAL_DEPTH:
-            raise RuntimeError(f"reference BVH depth {self.bvh_depth} overflows its 16-entry "
-                               "traversal stack")
+        if self.bvh_depth > self.stack_entries:
+            raise RuntimeError(f"reference BVH depth {self.bvh_depth} overflows its "
+                               f"{self.stack_entries}-entry traversal stack")
 
     def export(self):
         L = self.L

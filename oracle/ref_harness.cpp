@@ -37,6 +37,16 @@ __host__ __device__ bool rayIntersectsBox(Ray& ray, const float3& min, const flo
 /* Host-only harness: the device compilation pass sees an empty file body. */
 #ifndef __CUDA_ARCH__
 
+/* The traversal stack and bounce count the linked renderer.cu was compiled
+ * with: 16 and 6 as shipped (renderer.cu:289, 25/33); the Makefile's
+ * ref-deep target builds a copy with both raised and passes them here. */
+#ifndef CRT_REF_STACK
+#define CRT_REF_STACK 16
+#endif
+#ifndef CRT_REF_DEPTH
+#define CRT_REF_DEPTH 6
+#endif
+
 namespace {
 
 struct PhiloxStream {
@@ -247,10 +257,16 @@ __attribute__((visibility("default"))) void ref_export_textures(uint32_t* dims, 
     }
 }
 
+/* Traversal stack entries and maximum bounces of the linked estimator. */
+__attribute__((visibility("default"))) void ref_limits(uint32_t out[2]) {
+    out[0] = CRT_REF_STACK;
+    out[1] = CRT_REF_DEPTH;
+}
+
 /* Closest hit through the reference's own traversal.  rays [n][8] =
  * o.xyz tmin d.xyz tmax; idx is the original face index, -1 on a miss, or
- * -2 when the ray's traversal would overflow the reference's 16-entry
- * stack (renderer.cu:289) and was therefore not run. */
+ * -2 when the ray's traversal would overflow the linked build's stack
+ * (16 entries as shipped, renderer.cu:289) and was therefore not run. */
 __attribute__((visibility("default"))) void ref_closest_hit(const float* rays, uint32_t n,
                                                             int32_t* idx, float* t, float* uv) {
     for (uint32_t k = 0; k < n; ++k) {
@@ -258,7 +274,7 @@ __attribute__((visibility("default"))) void ref_closest_hit(const float* rays, u
         Ray ray(make_float3(r[0], r[1], r[2]), make_float3(r[4], r[5], r[6]));
         ray.tMin = r[3];
         ray.tMax = r[7];
-        if (stack_need(g_scene->getBvhPtr(), ray) > 16) {
+        if (stack_need(g_scene->getBvhPtr(), ray) > CRT_REF_STACK) {
             idx[k] = -2;
             t[k] = FLT_MAX;
             uv[2 * k] = uv[2 * k + 1] = 0.f;
