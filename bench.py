@@ -17,13 +17,21 @@ max depth 8.  One step renders the whole frame (531M path samples).
   (BVH build + uploads) + crt_render_create + crt_render_pass +
   crt_render_resolve, wall clock.
 * roofline: the dominant stage of a profiled pass (per-launch CUDA events,
-  node and triangle fetches counted by an untimed re-run) against the
-  measured HBM copy bandwidth.
+  node and triangle fetches counted by an untimed re-run) against the L2
+  gather ceiling measured live by crt_measure_gather (node- and triangle-
+  sized records at random indices of a 64 MiB working set, L2 only); its
+  DRAM part (ncu traffic per ray) against the measured HBM copy bandwidth.
 * cpu_baseline / --impl reference: the CPU oracle port of the reference's
   `--cpu` path on all host threads over a bounded pixel sample.
 
-Under torchrun each rank renders its own sample range of the same frame
-(weak scaling, no collective on the data path).
+Under torchrun each rank renders its own sample range of one frame (rank r:
+samples [r*spp, (r+1)*spp), weak scaling) and the step ends with one sum of
+the ranks' FP32 accumulators (NCCL all_reduce), the only exchange.
+
+The JSON line carries the headline figures first; per-stage timings, the
+autotuner's candidates and the inversion's details go to a second file,
+bench_detail.json (in the directory named by --detail-dir, default
+gpurun_out/ when it exists, else the working directory).
 """
 from __future__ import annotations
 
@@ -54,6 +62,31 @@ def measured_peaks():
         d = json.load(open(p))
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def gather_ceiling(torch, stream, record_sizes, working_set=64 << 20, l1=False, loads=256, repeats=5):
+    """GB/s of random record gathers (crt_measure_gather) from a working set
+    resident in L2 (64 MiB, half the L2): one figure per record size,
+    best of `repeats` launches of 1216 blocks x 256 threads (8 per SM on
+    152 SMs), each thread fetching `loads` records.  Bytes = records x size."""
+    from cudart_gb300 import measure_gather
+    buf = torch.ones(working_set // 4, dtype=torch.float32, device="cuda")
+    n_threads = 1216 * 256
+    out = {}
+    for rb in record_sizes:
+        measure_gather(buf, rb, n_threads, 8, l1=l1, stream=stream.cuda_stream)   # warm: data into L2
+        best = None
+        for _ in range(repeats):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            measure_gather(buf, rb, n_threads, loads, l1=l1, stream=stream.cuda_stream)
+            e.record(stream)
+            e.synchronize()
+            ms = s.elapsed_time(e)
+            best = ms if best is None else min(best, ms)
+        out[rb] = n_threads * loads * rb / (best * 1e-3) / 1e9
+    del buf
+    return out
 
 
 class ClockSampler:
@@ -256,13 +289,78 @@ def adjoint_leg(args, torch, stream):
                        "512x512, 64 spp, depth 6",
            "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3), "ratio": round(a_ms / f_ms, 3),
            "roulette": "survival probability held constant (unbiased gradient of the expected image)"}
-    # inversion
+    out["inversion"] = run_inversion(torch, g, r, sc, target, kd_true, boxes, args.inversion_iters,
+                                     loss=args.inversion_loss, exact=False)
+    vis = box_visibility(torch, g, sc, boxes)
+    err = np.array(out["inversion"]["albedo_rmse_per_box"])
+    seen = vis >= 100
+    out["inversion"]["visible_pixels_per_box"] = vis.tolist()
+    out["inversion"]["albedo_rmse_end_visible"] = (round(float(np.sqrt(np.mean(err[seen] ** 2))), 4)
+                                                   if seen.any() else None)
+    out["inversion"]["visible_boxes"] = int(seen.sum())
+    return out
+
+
+def box_visibility(torch, g, sc, mats):
+    """Pixels whose centre's camera ray first hits each material in `mats`
+    (pinhole camera of the scene; crt_trace_closest)."""
+    import numpy as np
+    from cudart_gb300 import camera_from_json
+    c = camera_from_json(sc.camera, sc.width, sc.height)
+    eye, d, up, right = (np.array(v[:], np.float64) for v in (c.eye, c.dir, c.up, c.right))
+    ys, xs = np.mgrid[0:sc.height, 0:sc.width]
+    nx = (2.0 * (xs + 0.5) / sc.width - 1.0).ravel()
+    ny = (1.0 - 2.0 * (ys + 0.5) / sc.height).ravel()
+    dirs = d[None] + right[None] * (c.fov * c.aspect) * nx[:, None] + up[None] * c.fov * ny[:, None]
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rays = np.zeros((len(dirs), 8), np.float32)
+    rays[:, :3] = eye
+    rays[:, 3] = 1e-5
+    rays[:, 4:7] = dirs
+    rays[:, 7] = np.finfo(np.float32).max
+    face, _, _ = g.trace_closest(torch.from_numpy(rays).cuda())
+    face = face.cpu().numpy()
+    mat = np.where(face >= 0, np.asarray(sc.material_ids)[np.maximum(face, 0)], -1)
+    return np.array([int(np.sum(mat == m)) for m in mats])
+
+
+def run_inversion(torch, g, r, sc, target, kd_true, boxes, iters, loss="clamped", exact=False,
+                  snr_evals=8):
+    """Adam (lr 1e-2) on the box albedos from 0.5, one 64-spp render and one
+    adjoint on independent samples per iteration.  loss "clamped": L2 on the
+    image clamped to [0, 1] (gradient zero where the estimate saturates);
+    "hdr": plain L2 on the radiance.  exact: exact-roulette adjoint.  Also
+    the gradient's signal-to-noise ratio per box at the start (mean over
+    `snr_evals` independent adjoints / their spread)."""
+    import numpy as np
+    n_mats = len(sc.materials)
+    npix = sc.width * sc.height
+    adj = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    gkd = torch.zeros((n_mats, 3), dtype=torch.float32, device="cuda")
+    gka = torch.zeros((n_mats, 3), dtype=torch.float32, device="cuda")
     kd = kd_true.copy()
     kd[boxes] = 0.5
     m1 = np.zeros_like(kd)
     m2 = np.zeros_like(kd)
     b1, b2, lr, eps = 0.9, 0.999, 1e-2, 1e-8
     err0 = float(np.sqrt(np.mean((kd[boxes] - kd_true[boxes]) ** 2)))
+
+    def grad_at(kd_vals, it, spp0_adj):
+        g.set_materials(kd=kd_vals)
+        r.restart(it * sc.spp)
+        r.render(sc.spp)
+        img = torch.from_numpy(r.accum()).cuda() / sc.spp
+        if loss == "clamped":
+            diff = img.clamp(0, 1) - target.clamp(0, 1)
+            adj[:, :3] = 2.0 * diff * (img < 1).float() / sc.spp
+        else:
+            diff = img - target
+            adj[:, :3] = 2.0 * diff / sc.spp
+        gkd.zero_()
+        gka.zero_()
+        r.adjoint(spp0_adj, sc.spp, adj.data_ptr(), gkd.data_ptr(), gka.data_ptr(), exact_roulette=exact)
+        r.synchronize()
+        return float((diff ** 2).sum()), gkd.cpu().numpy()
 
     def image_loss(kd_vals):
         """L2 image loss of a 1024-spp render (its own sample range) against
@@ -272,57 +370,72 @@ def adjoint_leg(args, torch, stream):
         r.restart(1 << 25)   # not the target's samples (1 << 24) nor the iterations'
         r.render(1024)
         img = torch.from_numpy(r.accum()).cuda() / 1024
-        return float(((img.clamp(0, 1) - target.clamp(0, 1)) ** 2).sum())
+        if loss == "clamped":
+            return float(((img.clamp(0, 1) - target.clamp(0, 1)) ** 2).sum())
+        return float(((img - target) ** 2).sum())
 
+    # gradient SNR at the start point: independent 64-spp adjoints
+    gs = np.array([grad_at(kd, 10000 + k, (1 << 22) + k * sc.spp)[1][boxes] for k in range(snr_evals)])
+    snr = np.abs(gs.mean(0)) / np.maximum(gs.std(0, ddof=1), 1e-30)
     clean0 = image_loss(kd)
     losses = []
     t0 = time.perf_counter()
-    for it in range(args.inversion_iters):
-        g.set_materials(kd=kd)
-        r.restart(it * sc.spp)
-        r.render(sc.spp)
-        img = torch.from_numpy(r.accum()).cuda() / sc.spp
-        # L2 on display-range radiance (clamped to [0, 1], as the RGBA8 output
-        # quantises it): the unbounded HDR loss is dominated by a few
-        # fireflies near the lights
-        diff = img.clamp(0, 1) - target.clamp(0, 1)
-        loss = float((diff ** 2).sum())
-        losses.append(loss)
-        adj[:, :3] = 2.0 * diff * (img < 1).float() / sc.spp
-        gkd.zero_()
-        gka.zero_()
-        r.adjoint((1 << 23) + it * sc.spp, sc.spp, adj.data_ptr(), gkd.data_ptr(), gka.data_ptr())
-        r.synchronize()
-        grad = gkd.cpu().numpy()
+    for it in range(iters):
+        loss_v, grad = grad_at(kd, it, (1 << 23) + it * sc.spp)
+        losses.append(loss_v)
         grad[np.setdiff1d(np.arange(n_mats), boxes)] = 0.0
         m1 = b1 * m1 + (1 - b1) * grad
         m2 = b2 * m2 + (1 - b2) * grad * grad
         step = lr * (m1 / (1 - b1 ** (it + 1))) / (np.sqrt(m2 / (1 - b2 ** (it + 1))) + eps)
         kd = np.clip(kd - step, 0.01, 0.99).astype(np.float32)
-        if it == 0:
-            loss0 = loss
     seconds = round(time.perf_counter() - t0, 2)
     clean1 = image_loss(kd)
     g.set_materials(kd=kd_true)
+    box_err = np.sqrt(np.mean((kd[boxes] - kd_true[boxes]) ** 2, axis=1))
     q = max(1, min(20, len(losses) // 4))
-    out["inversion"] = {"iterations": args.inversion_iters, "lr": lr, "loss_first": round(loss0, 4),
-                        "loss_last": round(loss, 4),
-                        "loss_median_first_iters": round(float(np.median(losses[:q])), 4),
-                        "loss_median_last_iters": round(float(np.median(losses[-q:])), 4),
-                        "image_loss_1024spp_start": round(clean0, 4),
-                        "image_loss_1024spp_end": round(clean1, 4),
-                        "albedo_rmse_start": round(err0, 4),
-                        "albedo_rmse_end": round(float(np.sqrt(np.mean((kd[boxes] - kd_true[boxes]) ** 2))), 4),
-                        "seconds": seconds,
-                        "note": "loss_first / loss_last are single noisy 64-spp iterations; the medians and "
-                                "the 1024-spp image losses (own samples) are the noise-robust measures"}
-    return out
+    return {"iterations": iters, "lr": lr, "loss": loss, "exact_roulette": exact,
+            "loss_median_first_iters": round(float(np.median(losses[:q])), 4),
+            "loss_median_last_iters": round(float(np.median(losses[-q:])), 4),
+            "image_loss_1024spp_start": round(clean0, 4), "image_loss_1024spp_end": round(clean1, 4),
+            "albedo_rmse_start": round(err0, 4),
+            "albedo_rmse_end": round(float(np.sqrt(np.mean(box_err ** 2))), 4),
+            "albedo_rmse_per_box": [round(float(x), 4) for x in box_err],
+            "grad_snr_per_box_start": [round(float(x), 3) for x in np.median(snr, axis=1)],
+            "seconds": seconds}
+
+
+def inversion_study(args):
+    """Material-inversion variants on the C5 workload: loss clamped / HDR,
+    constant-survival / exact-roulette adjoint; per-box errors, visibility
+    and gradient SNR.  One JSON line."""
+    import numpy as np
+    import torch
+    from cudart_gb300 import GB300Renderer, GB300Scene, scenes
+    sc = scenes.material_inversion()
+    g = GB300Scene(sc)
+    kd_true = np.array([m.kd for m in sc.materials], np.float32)
+    boxes = np.arange(4, len(sc.materials))
+    r = GB300Renderer(g, sc.width, sc.height, sc.spp, max_depth=sc.max_depth, seed=77, mode="wavefront")
+    r.restart(1 << 24)
+    r.render(1024)
+    target = torch.from_numpy(r.accum()).cuda() / 1024
+    vis = box_visibility(torch, g, sc, boxes)
+    out = {"visible_pixels_per_box": vis.tolist(), "variants": []}
+    for loss, exact in (("clamped", False), ("hdr", False), ("clamped", True), ("hdr", True)):
+        res = run_inversion(torch, g, r, sc, target, kd_true, boxes, args.inversion_iters, loss, exact)
+        err = np.array(res["albedo_rmse_per_box"])
+        for thr in (100, 1000):
+            m = vis >= thr
+            res[f"albedo_rmse_end_visible_{thr}px"] = round(float(np.sqrt(np.mean(err[m] ** 2))), 4) if m.any() else None
+        out["variants"].append(res)
+    print(json.dumps(out), flush=True)
 
 
 def run_gb300(args):
     import numpy as np
     import torch
     from cudart_gb300 import GB300Renderer, GB300Scene, autotune, options_dict, scenes
+    from cudart_gb300.sharding import reduce_accumulators, sample_range
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -360,33 +473,39 @@ def run_gb300(args):
                  "start_ms_per_spp": round(tune.start_ms_per_spp, 3),
                  "tuned_ms_per_spp": round(tune.ms_per_spp, 3)}
         opts = tune.options
-        opts.seed, opts.view_id = 1234, rank
+        opts.seed, opts.view_id = 1234, 0
         wf = GB300Renderer(scene, sc.width, sc.height, spp, options=opts)
     else:
-        # each rank renders its own Philox streams of the same frame (view_id = rank);
         # --options sets launch options by hand (e.g. to profile one variant)
         extra = json.loads(args.options) if args.options else {}
         wf = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
-                           mode="wavefront", view_id=rank, **extra)
+                           mode="wavefront", **extra)
     wf.set_stream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    # this rank's samples of the frame: [s0, s0 + spp) of world * spp
+    s0, s1 = sample_range(world * spp, rank, world)
+    assert s1 - s0 == spp
+
+    def step(r):
+        r.restart(s0)
+        r.render(spp)
+        if dist is not None:
+            reduce_accumulators(r.accum_tensor())
 
     def timed_steps(r, k_steps):
         durs = []
         for k in range(k_steps):
             flush.fill_(float(k))
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            r.reset()
             s.record(stream)
-            r.render(spp)
+            step(r)
             e.record(stream)
             durs.append((s, e))
         torch.cuda.synchronize()
         return [s.elapsed_time(e) for s, e in durs]
 
     for _ in range(args.warmup):
-        wf.reset()
-        wf.render(spp)
+        step(wf)
     barrier()
     with ClockSampler(local) as clk:
         barrier()
@@ -410,10 +529,9 @@ def run_gb300(args):
     identical = True
     for fmt in ("q8", "f32"):
         mk = GB300Renderer(scene, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
-                           mode="megakernel", view_id=rank, node_format=fmt)
+                           mode="megakernel", node_format=fmt)
         mk.set_stream(stream.cuda_stream)
-        mk.reset()
-        mk.render(spp)
+        step(mk)
         torch.cuda.synchronize()
         plain_by_format[fmt] = sum(timed_steps(mk, k_plain)) / k_plain
         identical = identical and bool(np.array_equal(mk.accum(), wf_acc))
@@ -423,6 +541,7 @@ def run_gb300(args):
     plain_value = npix * spp / (mk_ms * 1e-3) / 1e6
 
     out = None
+    detail = {}
     if rank == 0:
         # roofline: profiled pass of 8 spp (per-launch events, counted fetches)
         prof_r = GB300Renderer(scene, sc.width, sc.height, spp, options=wf.options)
@@ -451,21 +570,44 @@ def run_gb300(args):
             tr = json.load(open(tp)).get(main["kernel"], {}).get(fmt)
             if tr:
                 traffic = round(tr["dram_bytes_per_ray"] * main["rays"] / prof[f"{dom if dom in roof else 'extend'}_launches"])
-        roofline = {"bound": "hbm", "kernel": main["kernel"], "achieved": round(main["gbs"], 1),
-                    "peak": peak, "unit": "GB/s", "frac": round(main["gbs"] / peak, 4),
-                    "traffic": traffic, "peak_kind": f"{peak_kind} (HBM copy)",
-                    "algorithmic_bytes": f"nodes visited x {node_bytes} B + triangles tested x 48 B per ray",
-                    "dram_share_of_algorithmic": (round(traffic / main["bytes_per_launch"], 4)
-                                                  if traffic else None),
-                    "reading": "achieved counts the node and triangle bytes the traversal consumes; most are "
-                               "L1/L2 hits (traffic is the DRAM part), so frac can exceed 1: the kernel is "
-                               "issue/latency-bound, not HBM-bound",
-                    "stage_ms": {s: round(prof[f"{s}_ms"], 2) for s in stages},
-                    "profile_spp": 8,
-                    "extend_rays_by_bounce": prof["extend_rays_by_bounce"][:sc.max_depth],
-                    "extend_ms_by_bounce": [round(x, 3) for x in prof["extend_ms_by_bounce"][:sc.max_depth]],
-                    "stages": {k: {kk: (round(vv, 3) if isinstance(vv, float) else vv)
-                                   for kk, vv in v.items()} for k, v in roof.items()}}
+        # the ceiling of the bytes counted: gathers of node- and triangle-
+        # sized records from L2, weighted by the stage's byte mix
+        gc = gather_ceiling(torch, stream, (node_bytes, TRI_BYTES))
+        nb = prof["extension_nodes" if main["kernel"] == "wf_extend" else "shadow_nodes"] * node_bytes
+        tb = prof["extension_tris" if main["kernel"] == "wf_extend" else "shadow_tris"] * TRI_BYTES
+        l2_peak = (nb + tb) / (nb / gc[node_bytes] + tb / gc[TRI_BYTES])
+        gc_l1 = gather_ceiling(torch, stream, (node_bytes,), l1=True)
+        dram_gbs = traffic / (main["ms_per_launch"] * 1e-3) / 1e9 if traffic else None
+        roofline = {"bound": "l2", "kernel": main["kernel"], "achieved": round(main["gbs"], 1),
+                    "peak": round(l2_peak, 1), "unit": "GB/s", "frac": round(main["gbs"] / l2_peak, 4),
+                    "traffic": traffic,
+                    "peak_kind": "measured live: L2 gather ceiling (crt_measure_gather, 64 MiB, "
+                                 f"{node_bytes} B node / 48 B triangle records, weighted by the byte mix)",
+                    "hbm": {"achieved": round(dram_gbs, 1) if dram_gbs else None, "peak": peak,
+                            "frac": round(dram_gbs / peak, 4) if dram_gbs else None,
+                            "peak_kind": f"{peak_kind} HBM copy; achieved = ncu DRAM traffic / time"},
+                    "limiter": "latency and divergence: issue-active 66-79%, SIMT 10-12 of 32 lanes on "
+                               "bounces >= 1, long-scoreboard the top stall (ncu, "
+                               "profiles/wf_extend_large_textured_1080p.md)",
+                    "algorithmic_bytes": f"nodes visited x {node_bytes} B + triangles tested x 48 B per ray"}
+        step_bytes = None
+        if main["kernel"] == "wf_extend":
+            # per-step cross-check: all traversal bytes of a step / its time
+            per_ray_ext = (roof["extend"]["nodes_per_ray"] * node_bytes + roof["extend"]["tris_per_ray"] * TRI_BYTES)
+            per_ray_shd = (roof["shadow"]["nodes_per_ray"] * node_bytes + roof["shadow"]["tris_per_ray"] * TRI_BYTES)
+            step_bytes = ext * per_ray_ext + shd * per_ray_shd
+            roofline["step_check"] = {"traversal_bytes_per_step": round(step_bytes),
+                                      "gbs_over_whole_step": round(step_bytes / (ms_step * 1e-3) / 1e9, 1),
+                                      "within_ceiling": bool(step_bytes / (ms_step * 1e-3) / 1e9 <= l2_peak)}
+        detail["roofline"] = {
+            "gather_ceiling_l2_gbs": {str(k): round(v, 1) for k, v in gc.items()},
+            "gather_ceiling_l1_gbs": {str(k): round(v, 1) for k, v in gc_l1.items()},
+            "stage_ms": {s_: round(prof[f"{s_}_ms"], 2) for s_ in stages},
+            "profile_spp": 8,
+            "extend_rays_by_bounce": prof["extend_rays_by_bounce"][:sc.max_depth],
+            "extend_ms_by_bounce": [round(x, 3) for x in prof["extend_ms_by_bounce"][:sc.max_depth]],
+            "stages": {k: {kk: (round(vv, 3) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                       for k, v in roof.items()}}
         del prof_r
 
         # e2e: host arrays -> host image through the public API, with the BVH
@@ -540,33 +682,72 @@ def run_gb300(args):
         # overlapped schedule (once per bounce; the serial one folds it in)
         serial = bool(wf.options.flags & 8)
         launches = args.steps * waves * (3 + (4 if serial else 5) * sc.max_depth)
+        if tuned:
+            detail["autotune"] = tuned
+            tuned = {"options": tuned["options"], "seconds": tuned["seconds"]}
+        if c4:
+            detail["batched_views"] = c4
+            c4 = {k: c4[k] for k in ("speedup", "batched_wavefront", "sequential_plain", "samples_per_step",
+                                     "bvh_width", "workload")}
+        if c5:
+            detail["adjoint"] = c5
+            inv = c5["inversion"]
+            c5 = {k: c5[k] for k in ("forward_ms", "adjoint_ms", "ratio")}
+            c5["inversion"] = {k: inv[k] for k in ("iterations", "albedo_rmse_start", "albedo_rmse_end",
+                                                   "albedo_rmse_end_visible", "image_loss_1024spp_start",
+                                                   "image_loss_1024spp_end") if k in inv}
+        detail["e2e"] = e2e
+        e2e = {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step",
+                                   "seconds_per_step")}
+        detail["roofline_line"] = dict(roofline)
+        roofline = {k: roofline[k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac",
+                                             "traffic", "hbm", "step_check") if k in roofline}
+        roofline["hbm"] = {k: roofline["hbm"][k] for k in ("achieved", "peak", "frac")}
+        if c4:
+            c4 = {"speedup": c4["speedup"],
+                  "batched_msamples_per_s": c4["batched_wavefront"]["msamples_per_s"],
+                  "sequential_plain_msamples_per_s": c4["sequential_plain"]["msamples_per_s"],
+                  "spp_div": args.c4_spp_div}
+        # the standard keys first, the headline's own figures last: a reader
+        # of the line's last 1500 characters sees them whole
         out = {
             "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded generator: heightfield value noise, procedural texture)",
-            "config": {"workload": WORKLOAD, "mode": "wavefront (CUDA-graph waves, concurrent wave sets)",
-                       "width": sc.width, "height": sc.height, "spp": spp, "max_depth": sc.max_depth,
-                       "triangles": info.num_triangles, "bvh_nodes": info.num_nodes,
-                       "bvh_depth": info.max_depth, "autotune": tuned,
-                       "l2": "flushed before every step (256 MiB write); scene buffers > L2"},
-            "plain_kernel": {"value": round(plain_value, 3), "ms_per_step": round(mk_ms, 3),
-                             "node_format": plain_fmt,
-                             "ms_per_step_by_node_format": {k: round(v, 3) for k, v in plain_by_format.items()},
-                             "accum_identical_to_wavefront": identical},
-            "speedup_vs_plain": round(value / world / plain_value, 3),
+            "data": "synthetic (seeded generator)", "gpu_launches": launches,
+            "config": {"workload": "large_textured 1920x1080 256spp depth8, 2,174,986 triangles",
+                       "spp": spp, "max_depth": sc.max_depth, "bvh_nodes": info.num_nodes,
+                       "sharded": "sample ranges + all_reduce" if world > 1 else None,
+                       "l2": "flushed before every step (256 MiB write)"},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "e2e": e2e,
             "mrays_per_s": round(value * rays_per_sample, 1),
-            "rays_per_sample": round(rays_per_sample, 3),
+            "adjoint": c5, "batched_views": c4,
+            "plain_kernel": {"value": round(plain_value, 3), "node_format": plain_fmt,
+                             "identical": identical},
             "adjoint_forward_ratio": c5["ratio"] if c5 else None,
-            "batched_views": c4, "adjoint": c5,
-            "clocks": clocks, "gpu_launches": launches, "e2e": e2e, "roofline": roofline,
-            "cpu_baseline": cpu,
+            "speedup_vs_plain": round(value / world / plain_value, 3),
         }
+        detail["line_extra"] = {"rays_per_sample": round(rays_per_sample, 3), "autotune": tuned,
+                                "plain_ms_per_step_by_node_format": {k: round(v, 3) for k, v in plain_by_format.items()},
+                                "workload": WORKLOAD}
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     if out is not None:
+        write_detail(args, detail)
         print(json.dumps(out), flush=True)
+
+
+def write_detail(args, detail: dict) -> None:
+    """Per-stage timings, autotuner candidates and the legs' full records
+    (bench_detail.json); the JSON line keeps the headline figures."""
+    d = args.detail_dir or ("gpurun_out" if os.path.isdir("gpurun_out") else ".")
+    try:
+        os.makedirs(d, exist_ok=True)
+        with open(os.path.join(d, "bench_detail.json"), "w") as f:
+            json.dump(detail, f, indent=1)
+    except OSError:
+        pass
 
 
 def default_wave_paths(pixels: int) -> int:
@@ -614,13 +795,20 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch options, no autotuner")
     ap.add_argument("--options", default="", help='with --no-tune: launch options as JSON, e.g. {"node_format": "f32"}')
     ap.add_argument("--no-extra", action="store_true", help="skip the batched-views and adjoint legs")
-    ap.add_argument("--c4-spp-div", type=int, default=4, help="batched views: spp divisor")
+    ap.add_argument("--c4-spp-div", type=int, default=1,
+                    help="batched views: spp divisor (1 = the workload's own spp)")
+    ap.add_argument("--detail-dir", default="", help="directory for bench_detail.json")
     ap.add_argument("--inversion-iters", type=int, default=200)
+    ap.add_argument("--inversion-loss", default="clamped", choices=["clamped", "hdr"])
+    ap.add_argument("--inversion-study", action="store_true",
+                    help="run the material-inversion variants (loss, roulette mode) and exit")
     ap.add_argument("--build-only", choices=["gpu", "host"], default=None,
                     help="time crt_scene_create with this BVH builder on the 1080p scene and exit")
     args = ap.parse_args()
     if args.build_only:
         run_build_only(args)
+    elif args.inversion_study:
+        inversion_study(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

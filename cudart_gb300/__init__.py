@@ -6,10 +6,10 @@ reference's renderer interface plus the seeded synthetic workloads.
 """
 from ._lib import CrtError, load
 from .renderer import (GB300Batch, GB300Renderer, GB300Scene, autotune, bvh_build_host,
-                       camera_from_json, make_options, options_dict)
+                       camera_from_json, make_options, measure_gather, options_dict)
 from . import scenes
 from .ingest import SceneFiles, load_camera_json, load_png_texels, write_png
 
 __all__ = ["CrtError", "GB300Batch", "GB300Renderer", "GB300Scene", "autotune", "bvh_build_host",
            "camera_from_json", "load", "load_camera_json", "load_png_texels", "make_options",
-           "options_dict", "scenes", "SceneFiles", "write_png"]
+           "measure_gather", "options_dict", "scenes", "SceneFiles", "write_png"]

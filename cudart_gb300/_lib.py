@@ -117,6 +117,10 @@ FLAG_LANE_REFILL = 1
 FLAG_SPLIT_LEAF = 2
 FLAG_OCTANT_QUEUES = 4
 FLAG_SERIAL_SHADOW = 8
+FLAG_WINDOW_SORT = 16
+GATHER_L1 = 1
+SCENE_ERR_WATCHDOG = 1
+SCENE_ERR_STACK = 2
 
 
 # name -> (restype, argtypes); every entry point of include/crt_gb300.h
@@ -134,8 +138,10 @@ SIGNATURES = {
     "crt_scene_set_materials": (C.c_int, [P, P, U32]),
     "crt_scene_set_visit_limit": (C.c_int, [P, U32]),
     "crt_scene_clear_errors": (C.c_int, [P]),
+    "crt_scene_errors": (C.c_int, [P, P, P]),
     "crt_trace_closest": (C.c_int, [P, P, U32, P, P, P, P]),
     "crt_trace_counts": (C.c_int, [P, P, U32, P, P, P]),
+    "crt_measure_gather": (C.c_int, [P, U64, U32, U32, U32, U32, P, P]),
     "crt_render_options_default": (None, [P]),
     "crt_render_create": (C.c_int, [P, P, U32, U32, P, P]),
     "crt_render_destroy": (C.c_int, [P]),

@@ -489,6 +489,18 @@ int crt_scene_clear_errors(crt_scene s) {
     return CRT_OK;
 }
 
+static_assert(ERR_WATCHDOG == CRT_SCENE_ERR_WATCHDOG && ERR_STACK == CRT_SCENE_ERR_STACK,
+              "device error bits and their public names");
+
+int crt_scene_errors(crt_scene s, void* stream, uint32_t* bits) {
+    if (!s || !bits) return set_error(CRT_ERR_INVALID, "crt_scene_errors: null argument");
+    uint32_t w = 0;
+    CRT_CUDA(cudaMemcpyAsync(&w, s->error.p, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CRT_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    *bits = w & (CRT_SCENE_ERR_WATCHDOG | CRT_SCENE_ERR_STACK);
+    return CRT_OK;
+}
+
 int crt_scene_set_materials(crt_scene s, const crt_material* materials, uint32_t n) {
     if (!s || !materials) return set_error(CRT_ERR_INVALID, "crt_scene_set_materials: null argument");
     if (n != s->n_mats) return set_error(CRT_ERR_INVALID, "crt_scene_set_materials: material count differs");

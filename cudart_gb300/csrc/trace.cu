@@ -39,6 +39,31 @@ __global__ void __launch_bounds__(kTraceBlock) trace_closest_kernel(DevScene S, 
     }
 }
 
+// Gather ceiling: every thread fetches `loads` records of `rec16` float4s at
+// indices from its own LCG (independent of the loaded data, so many fetches
+// are in flight), through L2 only (.cg) or through L1 as the traversal's
+// __ldg fetches go (.nc).  The XOR of what was read goes to sink[thread] so
+// that no load is dropped.
+template <bool L1>
+__global__ void __launch_bounds__(256) gather_kernel(const float4* __restrict__ base, uint64_t records,
+                                                     uint32_t rec16, uint32_t loads,
+                                                     uint32_t* __restrict__ sink) {
+    const uint32_t tid = blockIdx.x * 256u + threadIdx.x;
+    uint32_t state = tid * 2654435761u + 12345u;
+    uint32_t acc = 0;
+    for (uint32_t k = 0; k < loads; ++k) {
+        state = state * 1664525u + 1013904223u;
+        const uint64_t r = ((uint64_t)state * records) >> 32;   // < records
+        const float4* p = base + r * rec16;
+#pragma unroll 4
+        for (uint32_t j = 0; j < rec16; ++j) {
+            const float4 v = L1 ? __ldg(p + j) : __ldcg(p + j);
+            acc ^= __float_as_uint(v.x) ^ __float_as_uint(v.y) ^ __float_as_uint(v.z) ^ __float_as_uint(v.w);
+        }
+    }
+    sink[tid] = acc;
+}
+
 int grid_for(uint32_t n, int block, int per_sm) {
     static int sms = 0;
     if (!sms) {
@@ -80,6 +105,24 @@ int crt_trace_counts(crt_scene s, const float* d_rays, uint32_t n, uint32_t* d_n
     auto k = s->default_f32 ? trace_closest_kernel<true, true> : trace_closest_kernel<true, false>;
     k<<<grid_for(n, kTraceBlock, 16), kTraceBlock, 0, (cudaStream_t)stream>>>(
         s->view(s->default_f32), (const float4*)d_rays, n, nullptr, nullptr, nullptr, d_nodes, d_tris);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}
+
+int crt_measure_gather(const void* d_buf, uint64_t bytes, uint32_t record_bytes, uint32_t n_threads,
+                       uint32_t loads_per_thread, uint32_t flags, uint32_t* d_sink, void* stream) {
+    if (!d_buf || !d_sink) return set_error(CRT_ERR_INVALID, "crt_measure_gather: null argument");
+    if (((uintptr_t)d_buf & 15u) != 0) return set_error(CRT_ERR_INVALID, "buffer must be 16-byte aligned");
+    if (record_bytes == 0 || record_bytes % 16 != 0 || record_bytes > 4096)
+        return set_error(CRT_ERR_INVALID, "record_bytes must be a multiple of 16 in [16, 4096]");
+    const uint64_t records = bytes / record_bytes;
+    if (records == 0 || records > 0xFFFFFFFFull)
+        return set_error(CRT_ERR_INVALID, "buffer must hold between 1 and 2^32-1 records");
+    if (n_threads == 0 || n_threads % 256 != 0)
+        return set_error(CRT_ERR_INVALID, "n_threads must be a positive multiple of 256");
+    auto k = (flags & CRT_GATHER_L1) ? gather_kernel<true> : gather_kernel<false>;
+    k<<<n_threads / 256, 256, 0, (cudaStream_t)stream>>>((const float4*)d_buf, records, record_bytes / 16,
+                                                          loads_per_thread, d_sink);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
 }

@@ -47,7 +47,7 @@ struct Tuner {
     uint64_t wave_bytes(const crt_render_options& o) const {
         const uint64_t paths = o.wave_paths ? o.wave_paths : default_wave_paths((uint64_t)width * height);
         const uint64_t sets = o.wave_sets ? o.wave_sets : 3u;
-        return paths * sets * ((o.flags & CRT_FLAG_OCTANT_QUEUES) ? 192ull : 136ull);
+        return paths * sets * ((o.flags & CRT_FLAG_OCTANT_QUEUES) ? 196ull : 140ull);
     }
 
     // ms per sample per pixel of `o`, or a negative value when the candidate

@@ -58,7 +58,8 @@ enum Counter : uint32_t {
     C_FETCH_CNT = 7,    // work counter of the profiling count kernels
     C_OCT0 = 8,         // octant-binned queues: entries per octant of queue 0 (8 words)
     C_OCT1 = 16,        //                       and of queue 1 (8 words)
-    C_COUNT = 24
+    C_SQ = 24,          // window sort: shadow-order entries placed this bounce
+    C_COUNT = 25
 };
 
 // Profiling totals: extension rays, nodes, triangles; shadow rays, nodes, triangles.
@@ -122,6 +123,7 @@ struct WaveParams {
     float4* hit;        // t, face, u, v
     uint32_t* queue[2];
     float4* shadow;     // 3 float4 per request
+    uint32_t* shadow_q; // window sort: request slots in traversal order, else null
     uint32_t* counters;
     const uint4* waves; // first segment, segments, paths, accumulate entries
     const WaveSeg* segs;
@@ -313,12 +315,13 @@ CRT_D uint32_t find_segment(const WaveSeg* segs, uint32_t n, uint32_t i, bool by
     return lo;
 }
 
-// Warp-aggregated append into one of 8 regions: the lanes that want region
-// `key` share one atomic on counters[key]; returns this lane's slot in it.
-CRT_D uint32_t warp_append_keyed(uint32_t* counters, bool want, uint32_t key) {
+// Warp-aggregated append into one of `nkeys` regions: the lanes that want
+// region `key` share one atomic on counters[key]; returns this lane's slot in
+// it.
+CRT_D uint32_t warp_append_keyed(uint32_t* counters, bool want, uint32_t key, uint32_t nkeys = 8u) {
     const uint32_t active = __activemask();
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t peers = __match_any_sync(active, want ? key : 8u) & __ballot_sync(active, want);
+    const uint32_t peers = __match_any_sync(active, want ? key : nkeys) & __ballot_sync(active, want);
     uint32_t base = 0;
     const int leader = __ffs(peers) - 1;
     if (want && (int)lane == leader) base = atomicAdd(counters + key, __popc(peers));
@@ -374,6 +377,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_generate(WaveParams W) {
                 W.counters[(cur ? C_OCT0 : C_OCT1) + k] = 0;
             }
         W.counters[C_SHADOW] = 0;
+        W.counters[C_SQ] = 0;
         W.counters[C_FETCH_EXT] = 0;
         W.counters[C_FETCH_SHD] = 0;
     }
@@ -470,13 +474,95 @@ __global__ void __maxnreg__(F32 ? CRT_TRAVERSAL_REGS_F32 : CRT_TRAVERSAL_REGS) w
     count_rays(W.R.ray_counts, job.rays, 0);
 }
 
-// ADJ: the adjoint replay; the same bounce with gradient hooks, shared
-// memory [n_mats][6] floats.
+// One bounce of queue entry i (< n): loads the path, shades its hit (or
+// miss), stores the path back and reports whether it continues, its shadow
+// request and its next direction.  ADJ: the adjoint replay, the same bounce
+// with gradient hooks summed into grad_sh.
 template <bool ADJ>
+CRT_D void shade_entry(const WaveParams& W, const QueueView& q, uint32_t i, float* grad_sh, uint32_t& path,
+                       bool& alive, ShadowReq& sr, float3& dir) {
+    path = q.at(i);
+    const float4 o = W.st_o[path], d = W.st_d[path], c = W.st_c[path], m = W.st_m[path];
+    const float4 hv = W.hit[path];
+    const uint32_t pixel = __float_as_uint(o.w), sample = __float_as_uint(d.w);
+    const uint32_t pb = __float_as_uint(m.w);
+    const uint32_t view = pb >> kViewShift;
+    PathState ps;
+    ps.color = xyz(c);
+    ps.mask = xyz(m);
+    ps.prev = (int)(pb & 0xFFu);
+    ps.bounce = (pb >> kBounceShift) & ((1u << (kViewShift - kBounceShift)) - 1u);
+    ps.rng.init(W.R.seed, W.views[view].view_id, pixel, sample, __float_as_uint(c.w));
+    Ray ray;
+    ray.o = xyz(o);
+    ray.d = xyz(d);
+    Hit h;
+    h.t = hv.x;
+    h.face = __float_as_int(hv.y);
+    h.u = hv.z;
+    h.v = hv.w;
+    if (ADJ) {
+        const float4 wv = W.st_W[path];
+        WaveGrad g{grad_sh, xyz(wv), xyz(W.st_L[path])};
+        if (W.adj_exact) {
+            g.S = &W.R.S;
+            g.hist = W.adj_hist + (size_t)path * kHistMax;
+            g.meta = __float_as_uint(wv.w);
+            g.apply_pending(ps.color);
+        }
+        if (h.face < 0) {
+            shade_miss(ps);
+        } else {
+            alive = shade_hit(W.R, ps, ray, h, sr, &g) && ps.bounce < W.R.max_depth;
+        }
+        if (W.adj_exact) W.st_W[path].w = __uint_as_float(g.meta);
+    } else if (h.face < 0) {
+        shade_miss(ps);
+    } else {
+        alive = shade_hit(W.R, ps, ray, h, sr) && ps.bounce < W.R.max_depth;
+    }
+    store_state(W, path, ps, ray, pixel, sample, view);
+    dir = ray.d;
+}
+
+template <bool ADJ>
+CRT_D void write_shadow_request(const WaveParams& W, uint32_t ss, uint32_t path, const ShadowReq& sr) {
+    float4* e = W.shadow + 3ull * ss;
+    e[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, __uint_as_float(path));
+    e[1] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.t_light);
+    e[2] = make_float4(sr.contrib.x, sr.contrib.y, sr.contrib.z, __uint_as_float(sr.light_face));
+    if (ADJ) {
+        const float3 w = xyz(W.st_W[path]) * sr.dcontrib;
+        W.shd_grad[ss] = make_float4(w.x, w.y, w.z, __uint_as_float(sr.light_mat));
+    }
+}
+
+CRT_D uint32_t octant_of(float3 d) {
+    return (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
+}
+
+// Window sort: the block shades kSortWin consecutive queue entries, then
+// places its surviving paths in the next extension queue grouped by
+// direction bin (octant x dominant axis, 24 bins) and its shadow requests
+// grouped by light face (32 bins), so that a traversal warp takes rays that
+// start near one another (the window's entries come from one region of the
+// image) and head the same way, or go to the same light.  The order of
+// queue entries changes no result.
+constexpr uint32_t kSortIters = 8, kSortWin = kWaveBlock * kSortIters, kSortBins = 32;
+
+CRT_D uint32_t direction_bin(float3 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    const uint32_t dom = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
+    return octant_of(d) * 3u + dom;
+}
+
 // Register cap of the shade kernel: measured 64 slightly ahead of uncapped.
 #ifndef CRT_SHADE_REGS
 #define CRT_SHADE_REGS 64
 #endif
+// ADJ: the adjoint replay, dynamic shared memory [n_mats][6] floats.
+// SORT: window sort of both output queues (W.shadow_q set, no octant queues).
+template <bool ADJ, bool SORT>
 __global__ void __maxnreg__(ADJ ? CRT_SHADE_REGS + 32 : CRT_SHADE_REGS) wf_shade(WaveParams W) {
     extern __shared__ float grad_sh[];
     if (ADJ) zero_grad_block(grad_sh, W.n_mats);
@@ -485,76 +571,86 @@ __global__ void __maxnreg__(ADJ ? CRT_SHADE_REGS + 32 : CRT_SHADE_REGS) wf_shade
     __shared__ uint32_t pre_sh[9];
     const QueueView q = queue_view(W, cur, pre_sh);
     uint32_t* qn = W.queue[cur ^ 1u];
-    const uint32_t end = (n + 31u) & ~31u;   // whole warps stay converged for the ballots
-    for (uint32_t i = blockIdx.x * kWaveBlock + threadIdx.x; i < end; i += gridDim.x * kWaveBlock) {
-        bool alive = false, want_shadow = false;
-        uint32_t path = 0;
-        ShadowReq sr;
-        sr.valid = false;
-        uint32_t oct = 0;
-        if (i < n) {
-            path = q.at(i);
-            const float4 o = W.st_o[path], d = W.st_d[path], c = W.st_c[path], m = W.st_m[path];
-            const float4 hv = W.hit[path];
-            const uint32_t pixel = __float_as_uint(o.w), sample = __float_as_uint(d.w);
-            const uint32_t pb = __float_as_uint(m.w);
-            const uint32_t view = pb >> kViewShift;
-            PathState ps;
-            ps.color = xyz(c);
-            ps.mask = xyz(m);
-            ps.prev = (int)(pb & 0xFFu);
-            ps.bounce = (pb >> kBounceShift) & ((1u << (kViewShift - kBounceShift)) - 1u);
-            ps.rng.init(W.R.seed, W.views[view].view_id, pixel, sample, __float_as_uint(c.w));
-            Ray ray;
-            ray.o = xyz(o);
-            ray.d = xyz(d);
-            Hit h;
-            h.t = hv.x;
-            h.face = __float_as_int(hv.y);
-            h.u = hv.z;
-            h.v = hv.w;
-            if (ADJ) {
-                const float4 wv = W.st_W[path];
-                WaveGrad g{grad_sh, xyz(wv), xyz(W.st_L[path])};
-                if (W.adj_exact) {
-                    g.S = &W.R.S;
-                    g.hist = W.adj_hist + (size_t)path * kHistMax;
-                    g.meta = __float_as_uint(wv.w);
-                    g.apply_pending(ps.color);
-                }
-                if (h.face < 0) {
-                    shade_miss(ps);
-                } else {
-                    alive = shade_hit(W.R, ps, ray, h, sr, &g) && ps.bounce < W.R.max_depth;
-                    want_shadow = sr.valid;
-                }
-                if (W.adj_exact) W.st_W[path].w = __uint_as_float(g.meta);
-            } else if (h.face < 0) {
-                shade_miss(ps);
+    if (!SORT) {
+        const uint32_t end = (n + 31u) & ~31u;   // whole warps stay converged for the ballots
+        for (uint32_t i = blockIdx.x * kWaveBlock + threadIdx.x; i < end; i += gridDim.x * kWaveBlock) {
+            bool alive = false;
+            uint32_t path = 0;
+            ShadowReq sr;
+            sr.valid = false;
+            float3 dir = f3(0.f, 0.f, 0.f);
+            if (i < n) shade_entry<ADJ>(W, q, i, grad_sh, path, alive, sr, dir);
+            if (W.octant) {
+                const uint32_t oct = octant_of(dir);
+                const uint32_t slot = warp_append_keyed(&W.counters[cur ? C_OCT0 : C_OCT1], alive, oct);
+                if (alive) qn[(size_t)oct * W.capacity + slot] = path;
             } else {
-                alive = shade_hit(W.R, ps, ray, h, sr) && ps.bounce < W.R.max_depth;
-                want_shadow = sr.valid;
+                const uint32_t slot = warp_append(&W.counters[cur ^ 1u], alive);
+                if (alive) qn[slot] = path;
             }
-            store_state(W, path, ps, ray, pixel, sample, view);
-            oct = (signbit(ray.d.x) ? 1u : 0u) | (signbit(ray.d.y) ? 2u : 0u) | (signbit(ray.d.z) ? 4u : 0u);
+            const uint32_t ss = warp_append(&W.counters[C_SHADOW], sr.valid);
+            if (sr.valid) write_shadow_request<ADJ>(W, ss, path, sr);
         }
-        if (W.octant) {
-            const uint32_t slot = warp_append_keyed(&W.counters[cur ? C_OCT0 : C_OCT1], alive, oct);
-            if (alive) qn[(size_t)oct * W.capacity + slot] = path;
-        } else {
-            const uint32_t slot = warp_append(&W.counters[cur ^ 1u], alive);
-            if (alive) qn[slot] = path;
-        }
-        const uint32_t ss = warp_append(&W.counters[C_SHADOW], want_shadow);
-        if (want_shadow) {
-            float4* e = W.shadow + 3ull * ss;
-            e[0] = make_float4(sr.o.x, sr.o.y, sr.o.z, __uint_as_float(path));
-            e[1] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.t_light);
-            e[2] = make_float4(sr.contrib.x, sr.contrib.y, sr.contrib.z, __uint_as_float(sr.light_face));
-            if (ADJ) {
-                const float3 w = xyz(W.st_W[path]) * sr.dcontrib;
-                W.shd_grad[ss] = make_float4(w.x, w.y, w.z, __uint_as_float(sr.light_mat));
+    } else {
+        // per window entry: path, (extension bin << 16 | rank) or ~0,
+        // shadow slot, (shadow bin << 16 | rank) or ~0
+        __shared__ uint32_t s_path[kSortWin], s_ext[kSortWin], s_slot[kSortWin], s_shd[kSortWin];
+        __shared__ uint32_t s_cnt[2 * kSortBins];
+        for (uint32_t w0 = blockIdx.x * kSortWin; w0 < n; w0 += gridDim.x * kSortWin) {
+            if (threadIdx.x < 2 * kSortBins) s_cnt[threadIdx.x] = 0;
+            __syncthreads();
+            for (uint32_t it = 0; it < kSortIters; ++it) {
+                const uint32_t j = it * kWaveBlock + threadIdx.x, i = w0 + j;
+                bool alive = false;
+                uint32_t path = 0;
+                ShadowReq sr;
+                sr.valid = false;
+                float3 dir = f3(0.f, 0.f, 0.f);
+                if (i < n) shade_entry<ADJ>(W, q, i, grad_sh, path, alive, sr, dir);
+                const uint32_t ek = alive ? direction_bin(dir) : 0u;
+                const uint32_t sk = sr.valid ? (sr.light_face & (kSortBins - 1u)) : 0u;
+                const uint32_t er = warp_append_keyed(s_cnt, alive, ek, kSortBins);
+                const uint32_t sr_rank = warp_append_keyed(s_cnt + kSortBins, sr.valid, sk, kSortBins);
+                const uint32_t ss = warp_append(&W.counters[C_SHADOW], sr.valid);
+                if (sr.valid) write_shadow_request<ADJ>(W, ss, path, sr);
+                s_path[j] = path;
+                s_ext[j] = alive ? (ek << 16) | er : ~0u;
+                s_slot[j] = ss;
+                s_shd[j] = sr.valid ? (sk << 16) | sr_rank : ~0u;
             }
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                // exclusive scans of both bin counts, offset by the window's
+                // places in the two queues (one atomic each)
+                const uint32_t lane = threadIdx.x;
+                const uint32_t e = s_cnt[lane], sh = s_cnt[kSortBins + lane];
+                uint32_t ei = e, si = sh;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ei, o), b = __shfl_up_sync(0xFFFFFFFFu, si, o);
+                    if ((int)lane >= o) {
+                        ei += a;
+                        si += b;
+                    }
+                }
+                uint32_t eb = 0, sb = 0;
+                if (lane == 31) {
+                    if (ei) eb = atomicAdd(&W.counters[cur ^ 1u], ei);
+                    if (si) sb = atomicAdd(&W.counters[C_SQ], si);
+                }
+                eb = __shfl_sync(0xFFFFFFFFu, eb, 31);
+                sb = __shfl_sync(0xFFFFFFFFu, sb, 31);
+                s_cnt[lane] = eb + ei - e;
+                s_cnt[kSortBins + lane] = sb + si - sh;
+            }
+            __syncthreads();
+            for (uint32_t it = 0; it < kSortIters; ++it) {
+                const uint32_t j = it * kWaveBlock + threadIdx.x;
+                const uint32_t e = s_ext[j], sh = s_shd[j];
+                if (e != ~0u) qn[s_cnt[e >> 16] + (e & 0xFFFFu)] = s_path[j];
+                if (sh != ~0u) W.shadow_q[s_cnt[kSortBins + (sh >> 16)] + (sh & 0xFFFFu)] = s_slot[j];
+            }
+            __syncthreads();   // the next window reuses the shared arrays
         }
     }
     if (ADJ) flush_grad_block(W, grad_sh);
@@ -570,8 +666,8 @@ struct ShadowJob {
 
     CRT_D ShadowJob(const WaveParams& W_, Stack& st_, float* grad_ = nullptr) : W(W_), st(st_), grad(grad_) {}
     CRT_D void start(uint32_t i) {
-        entry = i;
-        const float4* e = W.shadow + 3ull * i;
+        entry = W.shadow_q ? W.shadow_q[i] : i;
+        const float4* e = W.shadow + 3ull * entry;
         const float4 b = e[1];
         T.init(xyz(e[0]), xyz(b), kEps, b.w, (int32_t)__float_as_uint(e[2].w), st, W.R.S.max_visits);
     }
@@ -662,6 +758,7 @@ __global__ void wf_flip(WaveParams W) {
     }
     W.counters[C_CUR] = cur ^ 1u;
     W.counters[C_SHADOW] = 0;
+    W.counters[C_SQ] = 0;
     W.counters[C_FETCH_EXT] = 0;
     W.counters[C_FETCH_SHD] = 0;
 }
@@ -686,6 +783,7 @@ __global__ void wf_flip_ext(WaveParams W) {
 
 __global__ void wf_flip_shadow(WaveParams W) {
     W.counters[C_SHADOW] = 0;
+    W.counters[C_SQ] = 0;
     W.counters[C_FETCH_SHD] = 0;
 }
 
@@ -839,6 +937,12 @@ void drop_wave_graphs(crt_render r) {
     }
 }
 
+// Window sort of the shade kernel's output queues: on with
+// CRT_FLAG_WINDOW_SORT unless the extension queues are octant-binned.
+static bool window_sort(uint32_t flags) {
+    return (flags & CRT_FLAG_WINDOW_SORT) && !(flags & CRT_FLAG_OCTANT_QUEUES);
+}
+
 static int alloc_set(WaveSet& S, uint32_t cap, bool octant) {
     WaveBuffers& B = S.buf;
     B.capacity = cap;
@@ -852,6 +956,7 @@ static int alloc_set(WaveSet& S, uint32_t cap, bool octant) {
     CRT_CUDA(B.queue_a.alloc(c * 4 * (octant ? 8 : 1)));
     CRT_CUDA(B.queue_b.alloc(c * 4 * (octant ? 8 : 1)));
     CRT_CUDA(B.shadow.alloc(c * 48));
+    CRT_CUDA(B.shadow_q.alloc(c * 4));
     CRT_CUDA(B.counters.alloc(C_COUNT * 4));
     CRT_CUDA(cudaMemset(B.counters.p, 0, C_COUNT * 4));
     CRT_CUDA(B.waves.alloc(kMaxWaves * sizeof(uint4)));
@@ -920,6 +1025,7 @@ static WaveParams wave_params(crt_render r, WaveSet& set) {
     W.top_nodes = staged_nodes(r->scene, r->opts);
     W.refill_busy = refill_busy(r->opts);
     W.octant = B.octant;
+    W.shadow_q = window_sort(r->opts.flags) ? B.shadow_q.as<uint32_t>() : nullptr;
     W.capacity = B.capacity;
     return W;
 }
@@ -929,7 +1035,9 @@ struct WaveGrids {
     int tblock;          // extend / shadow threads per block
     size_t tsmem;        // their dynamic shared memory (traversal stacks)
     WaveKernel extend, shadow, extend_count, shadow_count;
+    WaveKernel shade, shade_adj;   // forward and adjoint-replay bounce (window sort or not)
 };
+
 
 // Kernel choice and launch shapes, queried before a capture starts.
 static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32, uint32_t block, uint32_t depth,
@@ -939,6 +1047,9 @@ static WaveGrids wave_grids(uint32_t capacity, uint32_t flags, bool f32, uint32_
     g.shadow = shadow_kernel(flags, f32, top_nodes > 0);
     g.extend_count = f32 ? wf_extend_count<true> : wf_extend_count<false>;
     g.shadow_count = f32 ? wf_shadow_count<true> : wf_shadow_count<false>;
+    const bool sort = window_sort(flags);
+    g.shade = sort ? wf_shade<false, true> : wf_shade<false, false>;
+    g.shade_adj = sort ? wf_shade<true, true> : wf_shade<true, false>;
     g.tblock = (int)block;
     g.tsmem = (size_t)top_nodes * (f32 ? sizeof(Bvh8FloatNode) : sizeof(Bvh8Node)) + (size_t)block * depth * sizeof(uint2);
     cudaFuncSetAttribute((const void*)g.extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.tsmem);
@@ -973,7 +1084,7 @@ static void enqueue_wave_body(const WaveParams& W, const WaveGrids& G, uint32_t 
     for (uint32_t b = 0; b < max_depth; ++b) {
         G.extend<<<G.ext, G.tblock, G.tsmem, s>>>(W);
         if (!s2) {
-            wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
+            G.shade<<<G.gen, kWaveBlock, 0, s>>>(W);
             G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W);
             wf_flip<<<1, 1, 0, s>>>(W);
             continue;
@@ -982,7 +1093,7 @@ static void enqueue_wave_body(const WaveParams& W, const WaveGrids& G, uint32_t 
             cudaStreamWaitEvent(s, shadowed, 0);   // shadow(b - 1) is done
             wf_flip_shadow<<<1, 1, 0, s>>>(W);
         }
-        wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
+        G.shade<<<G.gen, kWaveBlock, 0, s>>>(W);
         cudaEventRecord(shaded, s);
         cudaStreamWaitEvent(s2, shaded, 0);
         G.shadow<<<G.shd, G.tblock, G.tsmem, s2>>>(W);
@@ -1210,7 +1321,7 @@ static AdjointGrids adjoint_grids(crt_render r, const WaveGrids& G) {
     a.shadow_smem = G.tsmem + gsm;
     a.shadow = uses_f32_nodes(r) ? wf_shadow_adj<true> : wf_shadow_adj<false>;
     cudaFuncSetAttribute((const void*)a.shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.shadow_smem);
-    cudaFuncSetAttribute((const void*)wf_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute((const void*)G.shade_adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)a.shade_smem);
     a.shd = persistent_grid((const void*)a.shadow, G.tblock, a.shadow_smem);
     return a;
@@ -1255,7 +1366,7 @@ static int capture_adjoint_graph(crt_render r, WaveSet& set, const float4* adj, 
         wf_generate<true><<<G.gen, kWaveBlock, 0, cap>>>(W);  // replay
         for (uint32_t b = 0; b < r->opts.max_depth; ++b) {
             G.extend<<<G.ext, G.tblock, G.tsmem, cap>>>(W);
-            wf_shade<true><<<G.gen, kWaveBlock, A.shade_smem, cap>>>(W);
+            G.shade_adj<<<G.gen, kWaveBlock, A.shade_smem, cap>>>(W);
             A.shadow<<<A.shd, G.tblock, A.shadow_smem, cap>>>(W);
             wf_flip<<<1, 1, 0, cap>>>(W);
         }
@@ -1373,7 +1484,7 @@ int wavefront_profile_pass(crt_render r, const std::vector<ViewWork>& work, crt_
                 out->extend_rays_by_bounce[bb] += counter(counter(C_CUR));
                 wf_reset_count_fetch<<<1, 1, 0, s>>>(W);
                 G.extend_count<<<G.cnt, kWaveBlock, 0, s>>>(W);
-                timed(2, [&] { wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W); });
+                timed(2, [&] { G.shade<<<G.gen, kWaveBlock, 0, s>>>(W); });
                 out->shadow_ms_by_bounce[bb] += timed(3, [&] { G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W); });
                 out->shadow_rays_by_bounce[bb] += counter(C_SHADOW);
                 wf_reset_count_fetch<<<1, 1, 0, s>>>(W);
@@ -1438,6 +1549,9 @@ static_assert(sizeof(WaveSeg) == 32 && sizeof(DevView) <= 256 && C_COUNT * 4 <= 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 // Device address of the scratch on each device, looked up once per device.
+// The address belongs to the device's primary context; a cudaDeviceReset
+// would unload the module and leave it stale (documented in the header: the
+// entry point is not used again after a reset).
 static std::mutex g_noalloc_mutex;
 static void* g_noalloc_addr[64] = {};
 
@@ -1491,6 +1605,11 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     if (opts) o = *opts;
     else crt_render_options_default(&o);
     if (int st = check_render_options(o)) return st;
+    // an error left by earlier work belongs to its caller: report it without
+    // clearing it, and launch nothing, so the final check sees only ours
+    if (cudaError_t pending = cudaPeekAtLastError())
+        return set_error(CRT_ERR_CUDA, std::string("crt_render_tile_noalloc: CUDA error pending from "
+                                                   "earlier work: ") + cudaGetErrorString(pending));
     void* base = nullptr;
     int st = noalloc_scratch(&base);
     if (st != CRT_OK) return st;
@@ -1542,7 +1661,7 @@ extern "C" int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera
     wf_generate<false><<<G.gen, kWaveBlock, 0, s>>>(W);
     for (uint32_t k = 0; k < o.max_depth; ++k) {
         G.extend<<<G.ext, G.tblock, G.tsmem, s>>>(W);
-        wf_shade<false><<<G.gen, kWaveBlock, 0, s>>>(W);
+        wf_shade<false, false><<<G.gen, kWaveBlock, 0, s>>>(W);
         G.shadow<<<G.shd, G.tblock, G.tsmem, s>>>(W);
         wf_flip<<<1, 1, 0, s>>>(W);
     }

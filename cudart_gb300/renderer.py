@@ -187,6 +187,13 @@ class GB300Scene:
         """Reset the scene's sticky device error word (after CRT_ERR_WATCHDOG)."""
         check(load().crt_scene_clear_errors(self.handle))
 
+    def errors(self, stream: Optional[int] = None) -> int:
+        """The scene's sticky device error word (SCENE_ERR_* bits) after the
+        work queued on `stream` (default: the default stream)."""
+        bits = C.c_uint32(0)
+        check(load().crt_scene_errors(self.handle, stream, C.byref(bits)))
+        return int(bits.value)
+
     def set_bvh_width(self, width: int) -> None:
         """Rebuild the BVH with 4 or 8 children per node (same geometry)."""
         check(load().crt_scene_set_bvh_width(self.handle, width))
@@ -321,6 +328,20 @@ class GB300Renderer:
         p = C.c_void_p()
         check(load().crt_render_accum_device(self.handle, C.byref(p)))
         return p.value
+
+    def accum_tensor(self):
+        """The device accumulator as a torch CUDA tensor [height*width, 4]
+        (rgb + unused), without a copy; valid while the handle lives.  Lets
+        the ranks of a sample-sharded render sum their accumulators in place
+        (cudart_gb300.sharding.reduce_accumulators)."""
+        import torch
+        ptr = self.accum_device_ptr()
+        n = self.height * self.width
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (n, 4), "typestr": "<f4", "data": (ptr, False),
+                                        "version": 2, "strides": None}
+        return torch.as_tensor(_View(), device="cuda")
 
     def synchronize(self) -> None:
         check(load().crt_render_synchronize(self.handle))
@@ -472,3 +493,20 @@ def autotune(scene: GB300Scene, width: int, height: int, camera: Optional[Camera
 
 def options_dict(o: RenderOptions) -> dict:
     return {name: getattr(o, name) for name, _ in o._fields_}
+
+
+def measure_gather(buf, record_bytes: int, n_threads: int, loads_per_thread: int, l1: bool = False,
+                   stream: Optional[int] = None):
+    """Queue one gather-ceiling launch (crt_measure_gather) over the CUDA
+    tensor `buf`: n_threads threads each fetch loads_per_thread records of
+    record_bytes from pseudo-random record indices, through L2 only or
+    (l1=True) through L1.  Returns the sink tensor; the bytes fetched are
+    n_threads * loads_per_thread * record_bytes.  Time it with events on
+    `stream` (default: the current stream)."""
+    import torch
+    sink = torch.empty(n_threads, dtype=torch.int32, device=buf.device)
+    s = stream if stream is not None else torch.cuda.current_stream(buf.device).cuda_stream
+    check(load().crt_measure_gather(buf.data_ptr(), buf.numel() * buf.element_size(), record_bytes,
+                                    n_threads, loads_per_thread, _lib.GATHER_L1 if l1 else 0,
+                                    sink.data_ptr(), s))
+    return sink

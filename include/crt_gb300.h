@@ -207,6 +207,17 @@ CRT_EXPORT int crt_scene_set_materials(crt_scene scene, const crt_material* mate
  * (the reference's traversal has no bound, renderer.cu:283-330). */
 CRT_EXPORT int crt_scene_set_visit_limit(crt_scene scene, uint32_t max_visits);
 CRT_EXPORT int crt_scene_clear_errors(crt_scene scene);
+/* Reads the scene's sticky device error word into *bits (CRT_SCENE_ERR_*;
+ * 0 when every traversal so far finished within its limits) after the work
+ * queued on `stream` (NULL = default stream) before this call: one 4-byte
+ * copy and a wait for that stream, nothing allocated.  The word is shared by
+ * every render of the scene, so a bit may come from any of them since the
+ * last crt_scene_clear_errors.  Callers of crt_render_tile_noalloc, which
+ * returns before its kernels run and never reads the word, use this to learn
+ * whether a tile had rays cut short. */
+#define CRT_SCENE_ERR_WATCHDOG 1u   /* a traversal passed the node-visit limit */
+#define CRT_SCENE_ERR_STACK 2u      /* a traversal stack overflowed */
+CRT_EXPORT int crt_scene_errors(crt_scene scene, void* stream, uint32_t* bits);
 /* Rebuilds the scene's BVH with 4 or 8 children per node from its own
  * triangle records (the geometry is unchanged, so every query answers the
  * same) and uploads it in place of the current one; the autotuner's BVH
@@ -237,6 +248,19 @@ CRT_EXPORT int crt_trace_closest(crt_scene scene, const float* d_rays, uint32_t 
 CRT_EXPORT int crt_trace_counts(crt_scene scene, const float* d_rays, uint32_t n, uint32_t* d_nodes,
                      uint32_t* d_tris, void* stream);
 
+/* Measurement aid with no counterpart in the reference: the ceiling of the
+ * traversal's access pattern.  n_threads (a multiple of 256) threads each
+ * fetch loads_per_thread records of record_bytes (a multiple of 16) from
+ * pseudo-random record indices of d_buf (bytes long, 16-byte aligned),
+ * through L2 only, or through L1 as node fetches go with CRT_GATHER_L1.
+ * d_sink gets one word per thread (keeps the loads live).  Bytes fetched =
+ * n_threads * loads_per_thread * record_bytes; time it with events on
+ * `stream`.  A working set below the L2 size gives the L2 gather ceiling. */
+#define CRT_GATHER_L1 1u
+CRT_EXPORT int crt_measure_gather(const void* d_buf, uint64_t bytes, uint32_t record_bytes,
+                                  uint32_t n_threads, uint32_t loads_per_thread, uint32_t flags,
+                                  uint32_t* d_sink, void* stream);
+
 /* ---- progressive render -------------------------------------------------
  * Replaces ParallelRenderer (src/include/renderer.h:102-126). */
 typedef enum {
@@ -258,10 +282,19 @@ enum {
                                    mostly holds rays of one octant: the same child
                                    order at every node.  8x the queue memory; not
                                    used by crt_render_tile_noalloc */
-    CRT_FLAG_SERIAL_SHADOW = 8u /* trace each bounce's shadow rays before the next
+    CRT_FLAG_SERIAL_SHADOW = 8u, /* trace each bounce's shadow rays before the next
                                    bounce's extension rays.  By default the two
                                    (independent) traversals are branches of the
                                    wave graph and fill each other's tails */
+    CRT_FLAG_WINDOW_SORT = 16u  /* the shade kernel groups each block's 1024
+                                   consecutive queue entries before appending
+                                   them: surviving paths by direction bin
+                                   (octant x dominant axis), shadow requests by
+                                   light face, so a traversal warp takes rays
+                                   from one image region heading one way.
+                                   4 more bytes per path; ignored with
+                                   CRT_FLAG_OCTANT_QUEUES and by
+                                   crt_render_tile_noalloc */
 };
 
 typedef struct {
@@ -447,7 +480,17 @@ CRT_EXPORT int crt_render_adjoint(crt_render r, uint32_t spp0, uint32_t n_spp, c
  * first call on a device looks up the scratch array's device address; make
  * that first call before any stream capture.  All calls share the one
  * scratch array, so calls that can overlap on the GPU (different streams,
- * or different threads without ordering) race: serialise them. */
+ * or different threads without ordering) race: serialise them.
+ * The call only queues kernels on `stream`: a traversal cut short by the
+ * scene's visit limit or a stack overflow sets the scene's error word, which
+ * this function does not read; check it with crt_scene_errors.  A CUDA error
+ * already pending on the calling thread from earlier work is reported
+ * (CRT_ERR_CUDA, not cleared) and nothing is launched.  The cached device
+ * address of the scratch belongs to the device's primary context: after
+ * cudaDeviceReset on that device, do not call this function again in the
+ * process.  CRT_FLAG_OCTANT_QUEUES is ignored here (the scratch holds
+ * single-region queues); like every launch option it does not change the
+ * sums. */
 #define CRT_NOALLOC_MAX_PATHS 65536u
 CRT_EXPORT int crt_render_tile_noalloc(crt_scene scene, const crt_camera* camera, uint32_t width,
                                        uint32_t height, const crt_render_options* opts,

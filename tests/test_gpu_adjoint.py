@@ -131,12 +131,15 @@ def test_exact_roulette_adjoint_matches_finite_differences(cuda):
         assert abs(np.median(diffs)) <= 0.02, (key, diffs)
 
 
-def test_octant_queues_give_the_same_gradient(cuda):
+@pytest.mark.parametrize("other", [4, 16])
+def test_queue_order_flags_give_the_same_gradient(cuda, other):
+    """Octant-binned queues (4) and the window sort (16) reorder the paths
+    the replay visits, not the paths themselves."""
     sc = scenes.material_inversion(width=64, height=64)
     adj = _adjoint_image(sc)
     g = GB300Scene(sc)
     out = []
-    for flags in (0, 4):
+    for flags in (0, other):
         r = GB300Renderer(g, sc.width, sc.height, 8, max_depth=6, seed=2, mode="wavefront", flags=flags,
                           wave_paths=1 << 16)
         out.append(_gpu_adjoint(cuda, r, len(sc.materials), adj, 0, 8))

@@ -43,7 +43,7 @@ def test_wavefront_equals_megakernel(cuda):
     assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("flags", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("flags", [1, 2, 3, 4, 5, 16, 17, 18, 20, 24])
 def test_scheduling_flags_do_not_change_results(cuda, flags):
     sc = scenes.cornell_box(width=96, height=64)
     a = _render(sc, 8, 5, "wavefront", wave_paths=1 << 15).accum()
@@ -82,6 +82,29 @@ def test_launch_shape_does_not_change_results(cuda, shape):
         r.render()
         out.append(r.accum())
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("extra", [{}, dict(node_format="f32", flags=8), dict(wave_sets=1, wave_paths=1 << 12)])
+def test_window_sort_renders_identically(cuda, extra):
+    """Grouping each window's survivors by direction and its shadow requests
+    by light (CRT_FLAG_WINDOW_SORT) reorders the queues only: four lights,
+    a texture, mirrors and glass, many windows and partial last windows."""
+    sc = scenes.large_textured(width=96, height=54, grid=64, tex_size=64, n_spheres=12,
+                               sphere_subdiv=2)
+    g = GB300Scene(sc)
+    out = []
+    for flags in (0, 16):
+        kw = dict(extra)
+        kw["flags"] = kw.get("flags", 0) | flags
+        r = GB300Renderer(g, sc.width, sc.height, 8, max_depth=8, mode="wavefront", **kw)
+        r.render()
+        out.append(r.accum())
+        ext, shd = r.ray_counts()
+        assert ext > 0 and shd > 0
+    assert np.array_equal(out[0], out[1])
+    mk = GB300Renderer(g, sc.width, sc.height, 8, max_depth=8, mode="megakernel")
+    mk.render()
+    assert np.array_equal(out[1], mk.accum())
 
 
 def test_four_wide_bvh_renders_identically(cuda):
