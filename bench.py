@@ -66,9 +66,10 @@ def measured_peaks():
 
 def gather_ceiling(torch, stream, record_sizes, working_set=64 << 20, l1=False, loads=256, repeats=5):
     """GB/s of random record gathers (crt_measure_gather) from a working set
-    resident in L2 (64 MiB, half the L2): one figure per record size,
-    best of `repeats` launches of 1216 blocks x 256 threads (8 per SM on
-    152 SMs), each thread fetching `loads` records.  Bytes = records x size."""
+    of `working_set` bytes (64 MiB: resident in L2, half its size; 96 KiB:
+    resident in every SM's L1 when l1): one figure per record size, best of
+    `repeats` launches of 1216 blocks x 256 threads (8 per SM on 152 SMs),
+    each thread fetching `loads` records.  Bytes = records x size."""
     from cudart_gb300 import measure_gather
     buf = torch.ones(working_set // 4, dtype=torch.float32, device="cuda")
     n_threads = 1216 * 256
@@ -228,11 +229,14 @@ def batched_views_leg(args, torch, stream):
         torch.cuda.synchronize()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record(stream)
+        t_host = time.perf_counter()
         b.render()
+        host_ms = (time.perf_counter() - t_host) * 1e3   # the host has queued every wave
         e.record(stream)
         torch.cuda.synchronize()
         ms = s.elapsed_time(e)
-        res[name] = {"ms": round(ms, 2), "msamples_per_s": round(samples / (ms * 1e-3) / 1e6, 2)}
+        res[name] = {"ms": round(ms, 2), "msamples_per_s": round(samples / (ms * 1e-3) / 1e6, 2),
+                     "host_enqueue_ms": round(host_ms, 2)}
         del b
     plain = max(("sequential_plain_q8", "sequential_plain_f32"), key=lambda k: res[k]["msamples_per_s"])
     res["sequential_plain"] = dict(res[plain], node_format=plain.rsplit("_", 1)[1])
@@ -570,26 +574,41 @@ def run_gb300(args):
             tr = json.load(open(tp)).get(main["kernel"], {}).get(fmt)
             if tr:
                 traffic = round(tr["dram_bytes_per_ray"] * main["rays"] / prof[f"{dom if dom in roof else 'extend'}_launches"])
-        # the ceiling of the bytes counted: gathers of node- and triangle-
-        # sized records from L2, weighted by the stage's byte mix
-        gc = gather_ceiling(torch, stream, (node_bytes, TRI_BYTES))
+        # the ceiling of the bytes counted: random gathers of node- and
+        # triangle-sized records (crt_measure_gather, fetched through L1 as
+        # the traversal's loads are) from an L1-resident (96 KiB) and an
+        # L2-resident (64 MiB) working set, combined with the traversal's own
+        # L1 sector hit rate (ncu, profiles/wf_extend_cache.json):
+        # 1 / (h1 / BW_L1 + (1 - h1) / BW_L2), weighted by the byte mix
         nb = prof["extension_nodes" if main["kernel"] == "wf_extend" else "shadow_nodes"] * node_bytes
         tb = prof["extension_tris" if main["kernel"] == "wf_extend" else "shadow_tris"] * TRI_BYTES
-        l2_peak = (nb + tb) / (nb / gc[node_bytes] + tb / gc[TRI_BYTES])
-        gc_l1 = gather_ceiling(torch, stream, (node_bytes,), l1=True)
+        g1 = gather_ceiling(torch, stream, (node_bytes, TRI_BYTES), working_set=96 << 10, l1=True)
+        g2 = gather_ceiling(torch, stream, (node_bytes, TRI_BYTES), working_set=64 << 20, l1=True)
+        mix = lambda g: (nb + tb) / (nb / g[node_bytes] + tb / g[TRI_BYTES])
+        bw1, bw2 = mix(g1), mix(g2)
+        h1, h1_src = None, None
+        cp = os.path.join(ROOT, "profiles", "wf_extend_cache.json")
+        if os.path.exists(cp):
+            fmt = "f32" if wf.options.node_format == 1 else "q8"
+            ent = json.load(open(cp)).get(fmt, {})
+            if "l1_sector_hit" in ent:
+                h1, h1_src = float(ent["l1_sector_hit"]), "profiles/wf_extend_cache.json"
+        hier = 1.0 / (h1 / bw1 + (1.0 - h1) / bw2) if h1 is not None else bw2
         dram_gbs = traffic / (main["ms_per_launch"] * 1e-3) / 1e9 if traffic else None
-        roofline = {"bound": "l2", "kernel": main["kernel"], "achieved": round(main["gbs"], 1),
-                    "peak": round(l2_peak, 1), "unit": "GB/s", "frac": round(main["gbs"] / l2_peak, 4),
-                    "traffic": traffic,
-                    "peak_kind": "measured live: L2 gather ceiling (crt_measure_gather, 64 MiB, "
-                                 f"{node_bytes} B node / 48 B triangle records, weighted by the byte mix)",
+        roofline = {"bound": "l1+l2 gather" if h1 is not None else "l2 gather", "kernel": main["kernel"],
+                    "achieved": round(main["gbs"], 1), "peak": round(hier, 1), "unit": "GB/s",
+                    "frac": round(main["gbs"] / hier, 4), "traffic": traffic,
+                    "peak_kind": "measured live: crt_measure_gather, L1-resident and L2-resident working sets, "
+                                 f"{node_bytes} B node / 48 B triangle records by the byte mix, combined at the "
+                                 f"ncu L1 sector hit rate {h1} ({h1_src})",
+                    "l2_only": {"peak": round(bw2, 1), "frac": round(main["gbs"] / bw2, 4)},
                     "hbm": {"achieved": round(dram_gbs, 1) if dram_gbs else None, "peak": peak,
                             "frac": round(dram_gbs / peak, 4) if dram_gbs else None,
                             "peak_kind": f"{peak_kind} HBM copy; achieved = ncu DRAM traffic / time"},
-                    "limiter": "latency and divergence: issue-active 66-79%, SIMT 10-12 of 32 lanes on "
-                               "bounces >= 1, long-scoreboard the top stall (ncu, "
-                               "profiles/wf_extend_large_textured_1080p.md)",
+                    "limiter": "divergent dependent gathers: see profiles/wf_extend_large_textured_1080p.md "
+                               "(issue-active, SIMT lanes, long-scoreboard stalls)",
                     "algorithmic_bytes": f"nodes visited x {node_bytes} B + triangles tested x 48 B per ray"}
+        l2_peak = hier
         step_bytes = None
         if main["kernel"] == "wf_extend":
             # per-step cross-check: all traversal bytes of a step / its time
@@ -600,8 +619,8 @@ def run_gb300(args):
                                       "gbs_over_whole_step": round(step_bytes / (ms_step * 1e-3) / 1e9, 1),
                                       "within_ceiling": bool(step_bytes / (ms_step * 1e-3) / 1e9 <= l2_peak)}
         detail["roofline"] = {
-            "gather_ceiling_l2_gbs": {str(k): round(v, 1) for k, v in gc.items()},
-            "gather_ceiling_l1_gbs": {str(k): round(v, 1) for k, v in gc_l1.items()},
+            "gather_l1_resident_gbs": {str(k): round(v, 1) for k, v in g1.items()},
+            "gather_l2_resident_gbs": {str(k): round(v, 1) for k, v in g2.items()},
             "stage_ms": {s_: round(prof[f"{s_}_ms"], 2) for s_ in stages},
             "profile_spp": 8,
             "extend_rays_by_bounce": prof["extend_rays_by_bounce"][:sc.max_depth],
@@ -701,7 +720,7 @@ def run_gb300(args):
                                    "seconds_per_step")}
         detail["roofline_line"] = dict(roofline)
         roofline = {k: roofline[k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac",
-                                             "traffic", "hbm", "step_check") if k in roofline}
+                                             "traffic", "l2_only", "hbm", "step_check") if k in roofline}
         roofline["hbm"] = {k: roofline["hbm"][k] for k in ("achieved", "peak", "frac")}
         if c4:
             c4 = {"speedup": c4["speedup"],
@@ -783,7 +802,59 @@ def run_build_only(args) -> None:
                       "build_ms": round(statistics.median(build), 2), "steps": args.steps}))
 
 
+def _ref_load_once(obj: str, cam: str, tex: str, w: int, h: int) -> float:
+    """The reference's own loader (Scene::loadObj, loadCamera, loadTextures,
+    loadTriangles; oracle/_ref, built where the CudaRT sources are) in ms."""
+    import ctypes as C
+    L = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libcrt_ref.so"))
+    L.ref_time_load.restype = C.c_double
+    L.ref_time_load.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int]
+    return float(L.ref_time_load(obj.encode(), cam.encode(), tex.encode(), w, h))
+
+
+def run_ingest(args) -> None:
+    """Scene-file loading on the host: crt_scene_files_load +
+    crt_camera_load_json on the OBJ/MTL/JSON/PNG files of a workload (best of
+    --steps), beside the reference's loader on the same files as the CPU
+    baseline when oracle/_ref exists (one load, in a process of its own: the
+    reference keeps loader state in static variables).  One JSON line."""
+    from cudart_gb300 import SceneFiles, load_camera_json, scenes
+    sc = getattr(scenes, args.ingest)()
+    with tempfile.TemporaryDirectory() as td:
+        files = scenes.write_reference_files(sc, td, args.ingest)
+        obj_bytes = os.path.getsize(files["obj"])
+        lib_ms, parse_ms = [], []
+        for _ in range(max(1, args.steps)):
+            t = time.perf_counter()
+            f = SceneFiles(files["obj"], files["textures"])
+            load_camera_json(files["camera"], sc.width, sc.height)
+            lib_ms.append((time.perf_counter() - t) * 1e3)
+            parse_ms.append(float(f.info.parse_ms))
+            assert f.n_tris == sc.n_tris
+            f.close()
+        ref_ms = None
+        if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libcrt_ref.so")):
+            p = subprocess.run([sys.executable, os.path.abspath(__file__), "--ref-load-once", files["obj"],
+                                files["camera"], files["textures"], str(sc.width), str(sc.height)],
+                               capture_output=True, text=True, check=True)
+            ref_ms = float(p.stdout.strip().splitlines()[-1])
+    best = min(lib_ms)
+    print(json.dumps({"metric": "scene_files_load_ms", "scene": args.ingest, "triangles": sc.n_tris,
+                      "obj_mb": round(obj_bytes / 1e6, 1), "library_ms": round(best, 1),
+                      "library_parse_ms": round(min(parse_ms), 1),
+                      "library_mb_per_s": round(obj_bytes / 1e3 / best, 1),
+                      "cpu_baseline": None if ref_ms is None else {
+                          "value": round(ref_ms, 1), "unit": "ms", "kind": "reference", "cores": 1,
+                          "sample": "Scene::loadObj + loadCamera + loadTextures + loadTriangles, one load"},
+                      "speedup": None if ref_ms is None else round(ref_ms / best, 1),
+                      "host_threads": os.cpu_count()}), flush=True)
+
+
 def main():
+    if len(sys.argv) == 7 and sys.argv[1] == "--ref-load-once":
+        obj, cam, tex, w, h = sys.argv[2:]
+        print(_ref_load_once(obj, cam, tex, int(w), int(h)))
+        return
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -802,10 +873,14 @@ def main():
     ap.add_argument("--inversion-loss", default="clamped", choices=["clamped", "hdr"])
     ap.add_argument("--inversion-study", action="store_true",
                     help="run the material-inversion variants (loss, roulette mode) and exit")
+    ap.add_argument("--ingest", default=None, choices=["mixed_mid", "large_textured"],
+                    help="time scene-file loading of this workload on the host and exit")
     ap.add_argument("--build-only", choices=["gpu", "host"], default=None,
                     help="time crt_scene_create with this BVH builder on the 1080p scene and exit")
     args = ap.parse_args()
-    if args.build_only:
+    if args.ingest:
+        run_ingest(args)
+    elif args.build_only:
         run_build_only(args)
     elif args.inversion_study:
         inversion_study(args)

@@ -117,7 +117,7 @@ FLAG_LANE_REFILL = 1
 FLAG_SPLIT_LEAF = 2
 FLAG_OCTANT_QUEUES = 4
 FLAG_SERIAL_SHADOW = 8
-FLAG_WINDOW_SORT = 16
+FLAG_NO_WINDOW_SORT = 16
 GATHER_L1 = 1
 SCENE_ERR_WATCHDOG = 1
 SCENE_ERR_STACK = 2

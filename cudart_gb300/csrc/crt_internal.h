@@ -71,8 +71,7 @@ struct WaveBuffers {
     uint32_t capacity = 0;
     uint32_t seg_capacity = 0;      // wave segments the segs buffer holds
     bool octant = false;            // queues hold 8 octant regions
-    crt::DevBuf ray_o, ray_d, mask, color, hit, path_id, queue_a, queue_b, shadow, shadow_q, counters, waves,
-        segs, prof;
+    crt::DevBuf ray_o, color, hit, queue_a, queue_b, shadow, shadow_q, counters, waves, segs, prof;
     crt::DevBuf adj_L, adj_W, adj_shadow, adj_hist;   // adjoint replay state, allocated on first use
 };
 
@@ -174,7 +173,7 @@ inline int check_render_options(const crt_render_options& o) {
     if (o.top_nodes > 128) return set_error(CRT_ERR_INVALID, "top_nodes must be in [0, 128]");
     if (o.refill_busy > 31) return set_error(CRT_ERR_INVALID, "refill_busy must be in [0, 31]");
     if (o.flags & ~(uint32_t)(CRT_FLAG_LANE_REFILL | CRT_FLAG_SPLIT_LEAF | CRT_FLAG_OCTANT_QUEUES |
-                              CRT_FLAG_SERIAL_SHADOW | CRT_FLAG_WINDOW_SORT))
+                              CRT_FLAG_SERIAL_SHADOW | CRT_FLAG_NO_WINDOW_SORT))
         return set_error(CRT_ERR_INVALID, "unknown render flag");
     return CRT_OK;
 }

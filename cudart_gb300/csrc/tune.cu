@@ -131,10 +131,10 @@ struct Tuner {
                 }
             }
         }
-        // octant-binned queues
-        {
+        // queue order: octant-binned queues, and the shade kernel's window sort
+        for (uint32_t f : {(uint32_t)CRT_FLAG_OCTANT_QUEUES, (uint32_t)CRT_FLAG_NO_WINDOW_SORT}) {
             crt_render_options c = cur;
-            c.flags ^= CRT_FLAG_OCTANT_QUEUES;
+            c.flags ^= f;
             const float tc = measure(c);
             if (tc > 0.f && tc < t * (1.f - kAdoptMargin)) {
                 cur = c;

@@ -286,14 +286,15 @@ enum {
                                    bounce's extension rays.  By default the two
                                    (independent) traversals are branches of the
                                    wave graph and fill each other's tails */
-    CRT_FLAG_WINDOW_SORT = 16u  /* the shade kernel groups each block's 1024
-                                   consecutive queue entries before appending
-                                   them: surviving paths by direction bin
-                                   (octant x dominant axis), shadow requests by
-                                   light face, so a traversal warp takes rays
-                                   from one image region heading one way.
-                                   4 more bytes per path; ignored with
-                                   CRT_FLAG_OCTANT_QUEUES and by
+    CRT_FLAG_NO_WINDOW_SORT = 16u /* by default the shade kernel groups each
+                                   block's 1024 consecutive queue entries before
+                                   appending them: surviving paths by direction
+                                   (7 x 7 cells of the octahedral map), shadow
+                                   requests by light face, so that a traversal
+                                   warp takes rays from one image region heading
+                                   one way.  This flag appends in warp order
+                                   instead.  The sort is also off with
+                                   CRT_FLAG_OCTANT_QUEUES and in
                                    crt_render_tile_noalloc */
 };
 

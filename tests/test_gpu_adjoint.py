@@ -133,8 +133,8 @@ def test_exact_roulette_adjoint_matches_finite_differences(cuda):
 
 @pytest.mark.parametrize("other", [4, 16])
 def test_queue_order_flags_give_the_same_gradient(cuda, other):
-    """Octant-binned queues (4) and the window sort (16) reorder the paths
-    the replay visits, not the paths themselves."""
+    """Octant-binned queues (4) and appending without the window sort (16)
+    reorder the paths the replay visits, not the paths themselves."""
     sc = scenes.material_inversion(width=64, height=64)
     adj = _adjoint_image(sc)
     g = GB300Scene(sc)

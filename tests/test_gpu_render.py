@@ -87,8 +87,9 @@ def test_launch_shape_does_not_change_results(cuda, shape):
 @pytest.mark.parametrize("extra", [{}, dict(node_format="f32", flags=8), dict(wave_sets=1, wave_paths=1 << 12)])
 def test_window_sort_renders_identically(cuda, extra):
     """Grouping each window's survivors by direction and its shadow requests
-    by light (CRT_FLAG_WINDOW_SORT) reorders the queues only: four lights,
-    a texture, mirrors and glass, many windows and partial last windows."""
+    by light (the default; CRT_FLAG_NO_WINDOW_SORT = 16 turns it off)
+    reorders the queues only: four lights, a texture, mirrors and glass,
+    many windows and partial last windows."""
     sc = scenes.large_textured(width=96, height=54, grid=64, tex_size=64, n_spheres=12,
                                sphere_subdiv=2)
     g = GB300Scene(sc)
