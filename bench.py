@@ -324,7 +324,8 @@ def box_visibility(torch, g, sc, mats):
     rays[:, 7] = np.finfo(np.float32).max
     face, _, _ = g.trace_closest(torch.from_numpy(rays).cuda())
     face = face.cpu().numpy()
-    mat = np.where(face >= 0, np.asarray(sc.material_ids)[np.maximum(face, 0)], -1)
+    ids = np.asarray(sc.material_ids).astype(np.int64)
+    mat = np.where(face >= 0, ids[np.maximum(face, 0)], -1)
     return np.array([int(np.sum(mat == m)) for m in mats])
 
 
@@ -420,6 +421,7 @@ def inversion_study(args):
     kd_true = np.array([m.kd for m in sc.materials], np.float32)
     boxes = np.arange(4, len(sc.materials))
     r = GB300Renderer(g, sc.width, sc.height, sc.spp, max_depth=sc.max_depth, seed=77, mode="wavefront")
+    r.set_stream(torch.cuda.current_stream().cuda_stream)   # torch's adjoint buffers and the adjoint: one stream
     r.restart(1 << 24)
     r.render(1024)
     target = torch.from_numpy(r.accum()).cuda() / 1024
