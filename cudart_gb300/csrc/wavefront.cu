@@ -41,8 +41,10 @@ constexpr int kTraversalBlockMax = 256;    // extend / shadow: block size chosen
 #ifndef CRT_TRAVERSAL_REGS
 #define CRT_TRAVERSAL_REGS 56
 #endif
+// FP32 planes: 56 as well since the window sort (+0.6% on the 1080p frame,
+// +1.1% on the mixed scene over 64, 16 bytes of spill; 72 loses 2-3%).
 #ifndef CRT_TRAVERSAL_REGS_F32
-#define CRT_TRAVERSAL_REGS_F32 64              // FP32 planes hold more live values
+#define CRT_TRAVERSAL_REGS_F32 56
 #endif
 constexpr uint32_t kDefaultWaveSets = 3;
 constexpr uint32_t kMaxWaves = 1u << 16;   // descriptors uploaded per chunk
