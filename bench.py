@@ -334,7 +334,8 @@ def run_inversion(torch, g, r, sc, target, kd_true, boxes, iters, loss="clamped"
     """Adam (lr 1e-2) on the box albedos from 0.5, one 64-spp render and one
     adjoint on independent samples per iteration.  loss "clamped": L2 on the
     image clamped to [0, 1] (gradient zero where the estimate saturates);
-    "hdr": plain L2 on the radiance.  exact: exact-roulette adjoint.  Also
+    "masked": L2 on the radiance over the pixel-channels where the target is
+    below 1; "hdr": plain L2 on the radiance.  exact: exact-roulette adjoint.  Also
     the gradient's signal-to-noise ratio per box at the start (mean over
     `snr_evals` independent adjoints / their spread)."""
     import numpy as np
@@ -358,6 +359,11 @@ def run_inversion(torch, g, r, sc, target, kd_true, boxes, iters, loss="clamped"
         if loss == "clamped":
             diff = img.clamp(0, 1) - target.clamp(0, 1)
             adj[:, :3] = 2.0 * diff * (img < 1).float() / sc.spp
+        elif loss == "masked":
+            # L2 over the pixel-channels the target does not saturate: the
+            # mask is fixed, so no noisy estimate decides which terms count
+            diff = (img - target) * (target < 1).float()
+            adj[:, :3] = 2.0 * diff / sc.spp
         else:
             diff = img - target
             adj[:, :3] = 2.0 * diff / sc.spp
@@ -377,6 +383,8 @@ def run_inversion(torch, g, r, sc, target, kd_true, boxes, iters, loss="clamped"
         img = torch.from_numpy(r.accum()).cuda() / 1024
         if loss == "clamped":
             return float(((img.clamp(0, 1) - target.clamp(0, 1)) ** 2).sum())
+        if loss == "masked":
+            return float((((img - target) * (target < 1).float()) ** 2).sum())
         return float(((img - target) ** 2).sum())
 
     # gradient SNR at the start point: independent 64-spp adjoints
@@ -427,7 +435,7 @@ def inversion_study(args):
     target = torch.from_numpy(r.accum()).cuda() / 1024
     vis = box_visibility(torch, g, sc, boxes)
     out = {"visible_pixels_per_box": vis.tolist(), "variants": []}
-    for loss, exact in (("clamped", False), ("hdr", False), ("clamped", True), ("hdr", True)):
+    for loss, exact in (("clamped", False), ("masked", False), ("hdr", False), ("clamped", True), ("masked", True)):
         res = run_inversion(torch, g, r, sc, target, kd_true, boxes, args.inversion_iters, loss, exact)
         err = np.array(res["albedo_rmse_per_box"])
         for thr in (100, 1000):
@@ -872,7 +880,7 @@ def main():
                     help="batched views: spp divisor (1 = the workload's own spp)")
     ap.add_argument("--detail-dir", default="", help="directory for bench_detail.json")
     ap.add_argument("--inversion-iters", type=int, default=200)
-    ap.add_argument("--inversion-loss", default="clamped", choices=["clamped", "hdr"])
+    ap.add_argument("--inversion-loss", default="clamped", choices=["clamped", "masked", "hdr"])
     ap.add_argument("--inversion-study", action="store_true",
                     help="run the material-inversion variants (loss, roulette mode) and exit")
     ap.add_argument("--ingest", default=None, choices=["mixed_mid", "large_textured"],
