@@ -245,6 +245,55 @@ def batched_views_leg(args, torch, stream):
     return out
 
 
+def config_legs(args, torch, stream):
+    """The two other single-frame workloads at their own sizes: the Cornell
+    box (512^2, 16 spp, depth 5, 36 triangles) and the mixed-material scene
+    (1280x720, 128 spp, depth 8, 102,412 triangles).  Each frame on the
+    wavefront form (autotuned on the frame, BVH width included) and on the
+    plain kernel (faster node format), best of 3 after a warm-up, L2 flushed
+    before each; accumulators must agree bit for bit."""
+    import numpy as np
+    from cudart_gb300 import GB300Renderer, GB300Scene, autotune, scenes
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for name, sc in (("cornell_512", scenes.cornell_box()), ("mixed_720p", scenes.mixed_mid())):
+        g = GB300Scene(sc)
+        spp = sc.spp
+        tune = autotune(g, sc.width, sc.height, max_depth=sc.max_depth, trial_spp=min(16, spp), repeats=2,
+                        rounds=1, tune_bvh_width=True)
+        opts = tune.options
+        opts.seed, opts.view_id = 1234, 0
+        rs = {"wavefront": GB300Renderer(g, sc.width, sc.height, spp, options=opts)}
+        for fmt in ("q8", "f32"):
+            rs["plain_" + fmt] = GB300Renderer(g, sc.width, sc.height, spp, max_depth=sc.max_depth, seed=1234,
+                                               mode="megakernel", node_format=fmt)
+        ms, acc = {}, {}
+        for k, r in rs.items():
+            r.set_stream(stream.cuda_stream)
+            best = None
+            for rep in range(4):
+                flush.fill_(float(rep))
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                r.reset()
+                s.record(stream)
+                r.render(spp)
+                e.record(stream)
+                e.synchronize()
+                if rep:
+                    best = s.elapsed_time(e) if best is None else min(best, s.elapsed_time(e))
+            ms[k] = best
+            acc[k] = r.accum()
+        plain = min(("plain_q8", "plain_f32"), key=lambda k: ms[k])
+        n = sc.width * sc.height * spp
+        out[name] = {"value": round(n / (ms["wavefront"] * 1e-3) / 1e6, 1),
+                     "plain": round(n / (ms[plain] * 1e-3) / 1e6, 1),
+                     "vs_plain": round(ms[plain] / ms["wavefront"], 3),
+                     "identical": bool(all(np.array_equal(acc["wavefront"], a) for a in acc.values())),
+                     "bvh_width": tune.bvh_width}
+        del rs, g
+    return out
+
+
 def adjoint_leg(args, torch, stream):
     """C5: Cornell shell + 32 boxes at 512^2, 64 spp per iteration, depth 6.
     adjoint/forward: one adjoint pass (primal trace + replay, both on the GPU)
@@ -690,6 +739,7 @@ def run_gb300(args):
                                        "scene_build_s": round(host_build, 4)}}
 
         c4 = batched_views_leg(args, torch, stream) if world == 1 and not args.no_extra else None
+        c12 = config_legs(args, torch, stream) if world == 1 and not args.no_extra else None
         c5 = adjoint_leg(args, torch, stream) if world == 1 and not args.no_extra else None
 
         cpu = None
@@ -750,7 +800,7 @@ def run_gb300(args):
                        "l2": "flushed before every step (256 MiB write)"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "e2e": e2e,
             "mrays_per_s": round(value * rays_per_sample, 1),
-            "adjoint": c5, "batched_views": c4,
+            "adjoint": c5, "batched_views": c4, "configs": c12,
             "plain_kernel": {"value": round(plain_value, 3), "node_format": plain_fmt,
                              "identical": identical},
             "adjoint_forward_ratio": c5["ratio"] if c5 else None,
