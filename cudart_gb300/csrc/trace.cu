@@ -120,6 +120,7 @@ int crt_measure_gather(const void* d_buf, uint64_t bytes, uint32_t record_bytes,
         return set_error(CRT_ERR_INVALID, "buffer must hold between 1 and 2^32-1 records");
     if (n_threads == 0 || n_threads % 256 != 0)
         return set_error(CRT_ERR_INVALID, "n_threads must be a positive multiple of 256");
+    if (flags & ~CRT_GATHER_L1) return set_error(CRT_ERR_INVALID, "crt_measure_gather: unknown flag");
     auto k = (flags & CRT_GATHER_L1) ? gather_kernel<true> : gather_kernel<false>;
     k<<<n_threads / 256, 256, 0, (cudaStream_t)stream>>>((const float4*)d_buf, records, record_bytes / 16,
                                                           loads_per_thread, d_sink);

@@ -91,8 +91,24 @@ def test_empty_scene_and_null_args_are_rejected():
     assert _create(desc)[0] == 1
     assert _lib.load().crt_scene_create(None, None) == 1
     assert _lib.load().crt_trace_closest(None, None, 0, None, None, None, None) == 1
+    assert _lib.load().crt_scene_errors(None, None, None) == 1
     with pytest.raises(CrtError):
         _lib.check(1)
+
+
+def test_gather_measurement_arguments_are_checked():
+    """crt_measure_gather refuses bad shapes before it launches anything."""
+    L = _lib.load()
+    buf, sink = 4096, 8192          # stand-in addresses: never dereferenced on these paths
+    cases = [((None, 1 << 20, 208, 256, 1, 0, sink, None), "null argument"),
+             ((buf + 4, 1 << 20, 208, 256, 1, 0, sink, None), "16-byte aligned"),
+             ((buf, 1 << 20, 200, 256, 1, 0, sink, None), "multiple of 16"),
+             ((buf, 100, 208, 256, 1, 0, sink, None), "between 1 and"),
+             ((buf, 1 << 20, 208, 100, 1, 0, sink, None), "multiple of 256"),
+             ((buf, 1 << 20, 208, 256, 1, 6, sink, None), "unknown flag")]
+    for args, msg in cases:
+        assert L.crt_measure_gather(*args) == 1
+        assert msg in L.crt_last_error().decode(), (args, L.crt_last_error())
 
 
 def test_camera_from_json_matches_oracle():
