@@ -28,10 +28,10 @@ Under torchrun each rank renders its own sample range of one frame (rank r:
 samples [r*spp, (r+1)*spp), weak scaling) and the step ends with one sum of
 the ranks' FP32 accumulators (NCCL all_reduce), the only exchange.
 
-The JSON line carries the headline figures first; per-stage timings, the
-autotuner's candidates and the inversion's details go to a second file,
-bench_detail.json (in the directory named by --detail-dir, default
-gpurun_out/ when it exists, else the working directory).
+The JSON line carries the contract's keys first and the headline's own
+figures last; per-stage timings, the autotuner's candidates and the
+inversion's details go to a second file, bench_detail.json (in the
+directory named by --detail-dir, default the working directory).
 """
 from __future__ import annotations
 
@@ -820,7 +820,7 @@ def run_gb300(args):
 def write_detail(args, detail: dict) -> None:
     """Per-stage timings, autotuner candidates and the legs' full records
     (bench_detail.json); the JSON line keeps the headline figures."""
-    d = args.detail_dir or ("gpurun_out" if os.path.isdir("gpurun_out") else ".")
+    d = args.detail_dir or "."
     try:
         os.makedirs(d, exist_ok=True)
         with open(os.path.join(d, "bench_detail.json"), "w") as f:
