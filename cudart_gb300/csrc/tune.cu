@@ -41,9 +41,9 @@ struct Tuner {
     std::map<Key, float> seen;   // measured ms per sample per pixel
     uint32_t candidates = 0;
 
-    // Path-state bytes of a candidate: 136 bytes per path per wave set
-    // (five float4 records, two queue words, one shadow request), plus 56
-    // more with octant-binned queues.
+    // Path-state bytes of a candidate: 140 bytes per path per wave set (two
+    // 32-byte state records, the hit, two queue words, one shadow request and
+    // its shadow-queue word), plus 56 more with octant-binned queues.
     uint64_t wave_bytes(const crt_render_options& o) const {
         const uint64_t paths = o.wave_paths ? o.wave_paths : default_wave_paths((uint64_t)width * height);
         const uint64_t sets = o.wave_sets ? o.wave_sets : 3u;
@@ -115,7 +115,7 @@ struct Tuner {
             {&crt_render_options::block_size, {64, 128, 256}},
             {&crt_render_options::stack_depth, {8, 12, 16, 24}},
             {&crt_render_options::wave_sets, {1, 2, 3, 4}},
-            {&crt_render_options::wave_paths, {1u << 21, 1u << 22, 1u << 23, 1u << 24}},
+            {&crt_render_options::wave_paths, {1u << 21, 1u << 22, 1u << 23, 1u << 24, 1u << 25}},
             {&crt_render_options::queue_chunk, {32, 64, 128}},
             {&crt_render_options::top_nodes, {0, 9, 73}},
         };
@@ -199,7 +199,7 @@ void crt_tune_params_default(crt_tune_params* p) {
     p->repeats = 3;
     p->rounds = 2;
     p->tune_bvh_width = 1;
-    p->max_wave_bytes = 16ull << 30;
+    p->max_wave_bytes = 32ull << 30;
 }
 
 int crt_autotune(crt_scene scene, const crt_camera* camera, uint32_t width, uint32_t height,

@@ -518,7 +518,7 @@ typedef struct {
     uint32_t rounds;           /* coordinate-descent sweeps at most (0 = 2) */
     uint32_t tune_bvh_width;   /* nonzero: also try the other BVH width */
     uint64_t max_wave_bytes;   /* skip candidates whose path state exceeds this
-                                  (0 = 16 GiB) */
+                                  (0 = 32 GiB) */
 } crt_tune_params;
 
 typedef struct {
