@@ -528,7 +528,7 @@ def run_gb300(args):
     tuned = None
     if not args.no_tune:
         t0 = time.perf_counter()
-        tune = autotune(scene, sc.width, sc.height, max_depth=sc.max_depth, trial_spp=32, repeats=2,
+        tune = autotune(scene, sc.width, sc.height, max_depth=sc.max_depth, trial_spp=64, repeats=2,
                         rounds=1, tune_bvh_width=False)
         tuned = {"options": {k: v for k, v in options_dict(tune.options).items()
                              if k not in ("seed", "max_depth", "view_id")},
@@ -833,7 +833,7 @@ def default_wave_paths(pixels: int) -> int:
     """The library's default paths per wave set (default_wave_paths in
     cudart_gb300/csrc/crt_internal.h)."""
     cap = 1 << 16
-    while cap < pixels * 8 and cap < (1 << 24):
+    while cap < pixels * 16 and cap < (1 << 25):
         cap <<= 1
     return cap
 

@@ -145,19 +145,21 @@ inline uint32_t staged_nodes(const crt_scene_s* s, const crt_render_options& o) 
     return o.top_nodes < s->info.num_nodes ? o.top_nodes : s->info.num_nodes;
 }
 
-// Checks the fields every render entry point shares; CRT_OK or an error.
-// Default paths per wave set: about 8 samples of every pixel the handle
-// renders, rounded up to a power of two in [2^16, 2^24] (16M paths at
-// 1080p).  Longer waves balance the thin late bounces of one wave against
-// the heavy early bounces of the next; measured on the 1080p C3 frame with
-// 4 sets: 4M paths 890, 8M 906, 16M 915, 32M 919 Msamples/s.
+// Default paths in flight per wave set: about 16 samples of every pixel of
+// the handle's views, rounded up to a power of two in [2^16, 2^25] (32M paths
+// at 1080p, 4.7 GB of path state per set).  Longer waves balance the thin
+// late bounces of one wave against the heavy early bounces of the next;
+// measured on the 1080p frame with the window sort and 4 sets: 16M paths
+// 1,170, 32M 1,195 Msamples/s (before the sort: 4M 890, 8M 906, 16M 915,
+// 32M 919).
 inline uint32_t default_wave_paths(uint64_t pixels) {
-    const uint64_t want = pixels * 8;
+    const uint64_t want = pixels * 16;
     uint32_t cap = 1u << 16;
-    while (cap < want && cap < (1u << 24)) cap <<= 1;
+    while (cap < want && cap < (1u << 25)) cap <<= 1;
     return cap;
 }
 
+// Checks the fields every render entry point shares; CRT_OK or an error.
 inline int check_render_options(const crt_render_options& o) {
     if (o.max_depth == 0 || o.max_depth > 1024) return set_error(CRT_ERR_INVALID, "max_depth must be in [1, 1024]");
     if (o.mode > CRT_MODE_WAVEFRONT) return set_error(CRT_ERR_INVALID, "unknown mode");

@@ -307,9 +307,9 @@ typedef struct {
     uint32_t block_size;       /* wavefront traversal kernels: threads per block,
                                   64, 128 or 256 (0 = 128) */
     uint32_t wave_paths;       /* wavefront: paths in flight per wave set; 0 = about
-                                  8 samples of every pixel of the handle's views,
-                                  a power of two in [2^16, 2^24] (16M at 1080p:
-                                  ~2.2 GB of path state per set) */
+                                  16 samples of every pixel of the handle's views,
+                                  a power of two in [2^16, 2^25] (32M at 1080p:
+                                  ~4.7 GB of path state per set) */
     uint32_t flags;            /* CRT_FLAG_* */
     uint32_t wave_sets;        /* wavefront: waves in flight at once, each with its
                                   own buffers and stream, 0..8 (0 = default 3) */
