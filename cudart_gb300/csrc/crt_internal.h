@@ -124,6 +124,9 @@ struct crt_render_s {
     std::vector<WaveSet> sets;
     uint32_t scene_generation = 0;  // scene BVH the captured wave graphs point at
     cudaEvent_t pass_start = nullptr;
+    uint32_t graph_epoch = 0;       // bumped whenever a set's wave graph is captured
+    void* pass_graph = nullptr;     // a whole pass as one graph (wavefront.cu), or null
+    uint64_t pass_key = 0;          // waves, sets and epoch it was built for
     ~crt_render_s() { crt::destroy_wave_sets(this); }
 };
 

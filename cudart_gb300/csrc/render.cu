@@ -313,6 +313,7 @@ int crt_render_destroy(crt_render r) {
     if (!r) return CRT_OK;
     if (r->stream) cudaStreamSynchronize(r->stream);
     if (r->own_stream) cudaStreamDestroy(r->stream);
+    r->stream = nullptr;   // the handle's destructor must not touch it
     delete r;
     return CRT_OK;
 }

@@ -985,7 +985,16 @@ static void destroy_set(WaveSet& s) {
     s.stream = nullptr;
 }
 
+static void drop_pass_graph(crt_render r) {
+    delete static_cast<WaveGraph*>(r->pass_graph);
+    r->pass_graph = nullptr;
+    r->pass_key = 0;
+}
+
+// Callers have synchronised the handle's stream (which may be gone already:
+// crt_render_destroy destroys its own stream before the handle).
 void destroy_wave_sets(crt_render r) {
+    drop_pass_graph(r);
     for (WaveSet& s : r->sets) destroy_set(s);
     r->sets.clear();
     if (r->pass_start) cudaEventDestroy(r->pass_start);
@@ -995,6 +1004,8 @@ void destroy_wave_sets(crt_render r) {
 // Captured launches hold the camera, stream-independent buffers and
 // options of the moment; they are re-captured on the next pass.
 void drop_wave_graphs(crt_render r) {
+    if (r->stream) cudaStreamSynchronize(r->stream);
+    drop_pass_graph(r);
     for (WaveSet& s : r->sets) {
         if (s.stream) cudaStreamSynchronize(s.stream);
         drop_set_graphs(s);
@@ -1266,6 +1277,7 @@ static int capture_set_graph(crt_render r, WaveSet& set) {
     if (set.graph) return CRT_OK;
     WaveGraph* g = new WaveGraph();
     set.graph = g;
+    ++r->graph_epoch;   // a whole-pass graph built from the old one is stale
     const WaveParams W = wave_params(r, set);
     const WaveGrids G = wave_grids(r, set.buf.capacity);
     CRT_CUDA(cudaGetLastError());
@@ -1295,6 +1307,47 @@ static int capture_set_graph(crt_render r, WaveSet& set) {
     return CRT_OK;
 }
 
+// A whole pass as one graph: wave w is a copy of set (w % K)'s wave graph,
+// after that set's previous wave has advanced its wave counter; its
+// accumulate follows its body and the previous wave's accumulate (any set),
+// so pixels add their samples in sample order, as the stream schedule below
+// does, and the bodies of consecutive waves on different sets overlap.  The
+// handle replays it with one launch per pass while the number of waves, the
+// sets and their wave graphs stay the same (the wave descriptors are data:
+// each pass uploads its own).
+static int build_pass_graph(crt_render r, size_t n_waves, uint32_t K) {
+    WaveGraph* pg = new WaveGraph();
+    r->pass_graph = pg;
+    CRT_CUDA(cudaGraphCreate(&pg->graph, 0));
+    const WaveGrids G = wave_grids(r, r->sets[0].buf.capacity);
+    std::vector<cudaGraphNode_t> last(K, nullptr);
+    cudaGraphNode_t prev_acc = nullptr;
+    for (size_t w = 0; w < n_waves; ++w) {
+        const uint32_t k = (uint32_t)(w % K);
+        WaveSet& s = r->sets[k];
+        WaveParams W = wave_params(r, s);
+        cudaGraphNode_t body = nullptr, acc = nullptr, next = nullptr;
+        CRT_CUDA(cudaGraphAddChildGraphNode(&body, pg->graph, last[k] ? &last[k] : nullptr, last[k] ? 1 : 0,
+                                            static_cast<WaveGraph*>(s.graph)->graph));
+        void* args[] = {&W};
+        cudaKernelNodeParams kp{};
+        kp.func = (void*)wf_accumulate;
+        kp.gridDim = dim3((unsigned)G.acc);
+        kp.blockDim = dim3(256);
+        kp.kernelParams = args;
+        const cudaGraphNode_t acc_deps[2] = {body, prev_acc};
+        CRT_CUDA(cudaGraphAddKernelNode(&acc, pg->graph, acc_deps, prev_acc ? 2 : 1, &kp));
+        kp.func = (void*)wf_next_wave;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        CRT_CUDA(cudaGraphAddKernelNode(&next, pg->graph, &acc, 1, &kp));
+        last[k] = next;
+        prev_acc = acc;
+    }
+    CRT_CUDA(cudaGraphInstantiate(&pg->exec, pg->graph, 0));
+    return CRT_OK;
+}
+
 // A pass: wave w runs on set w % K.  Each set's stream replays its graph for
 // the wave body, then waits for the previous wave's accumulate (on whichever
 // set ran it) before accumulating, so every pixel adds its samples in sample
@@ -1321,6 +1374,22 @@ int wavefront_pass(crt_render r, const std::vector<ViewWork>& work) {
         }
     for (WaveSet& s : r->sets)
         if ((st = capture_set_graph(r, s)) != CRT_OK) return st;
+    if (plan.waves.size() <= chunk) {
+        // one upload of wave descriptors covers the pass: queue it and the
+        // whole pass as one graph on the handle's stream
+        for (uint32_t k = 0; k < K; ++k) {
+            slice_waves(plan, k, plan.waves.size(), K, mine, segs);
+            if (!mine.empty() && (st = upload_waves(r->sets[k], mine, segs, r->stream))) return st;
+        }
+        const uint64_t key = ((uint64_t)plan.waves.size() << 40) ^ ((uint64_t)K << 32) ^ r->graph_epoch;
+        if (!r->pass_graph || r->pass_key != key) {
+            drop_pass_graph(r);
+            if ((st = build_pass_graph(r, plan.waves.size(), K)) != CRT_OK) return st;
+            r->pass_key = key;
+        }
+        CRT_CUDA(cudaGraphLaunch(static_cast<WaveGraph*>(r->pass_graph)->exec, r->stream));
+        return CRT_OK;
+    }
     // the sets start after everything already queued on the handle's stream
     CRT_CUDA(cudaEventRecord(r->pass_start, r->stream));
     for (WaveSet& s : r->sets) CRT_CUDA(cudaStreamWaitEvent(s.stream, r->pass_start, 0));
