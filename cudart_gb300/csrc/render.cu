@@ -275,6 +275,7 @@ void crt_render_options_default(crt_render_options* o) {
     o->block_size = 0;
     o->wave_paths = 0;
     o->node_format = -1;        // the scene's default encoding
+    o->top_nodes = 9;           // the tree's top two levels staged in shared memory (+1% at 1080p)
 }
 
 int crt_render_create(crt_scene s, const crt_camera* cam, uint32_t width, uint32_t height,

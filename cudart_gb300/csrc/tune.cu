@@ -46,7 +46,7 @@ struct Tuner {
     // its shadow-queue word), plus 56 more with octant-binned queues.
     uint64_t wave_bytes(const crt_render_options& o) const {
         const uint64_t paths = o.wave_paths ? o.wave_paths : default_wave_paths((uint64_t)width * height);
-        const uint64_t sets = o.wave_sets ? o.wave_sets : 3u;
+        const uint64_t sets = o.wave_sets ? o.wave_sets : 4u;
         return paths * sets * ((o.flags & CRT_FLAG_OCTANT_QUEUES) ? 196ull : 140ull);
     }
 
@@ -179,7 +179,7 @@ crt_render_options explicit_options(const crt_render_options& in, const crt_scen
     o.stack_depth = traversal_stack(o);
     o.queue_chunk = queue_chunk(o);
     o.refill_busy = refill_busy(o);
-    if (!o.wave_sets) o.wave_sets = 3;
+    if (!o.wave_sets) o.wave_sets = 4;
     if (!o.wave_paths) o.wave_paths = default_wave_paths(pixels);
     o.node_format = uses_f32_nodes(s, o.node_format) ? CRT_NODES_F32 : CRT_NODES_Q8;
     return o;

@@ -46,7 +46,7 @@ constexpr int kTraversalBlockMax = 256;    // extend / shadow: block size chosen
 #ifndef CRT_TRAVERSAL_REGS_F32
 #define CRT_TRAVERSAL_REGS_F32 56
 #endif
-constexpr uint32_t kDefaultWaveSets = 3;
+constexpr uint32_t kDefaultWaveSets = 4;   // measured: 4 x 32M-path sets +1.2% over 3 at 1080p
 constexpr uint32_t kMaxWaves = 1u << 16;   // descriptors uploaded per chunk
 
 enum Counter : uint32_t {

@@ -234,7 +234,7 @@ class GB300Scene:
 def make_options(max_depth: int = 6, seed: int = 1234, mode: str = "megakernel", view_id: int = 0,
                  wave_paths: int = 0, flags: int = 0, wave_sets: int = 0, block_size: int = 0,
                  stack_depth: int = 0, node_format: Optional[str] = None, queue_chunk: int = 0,
-                 top_nodes: int = 0, refill_busy: int = 0,
+                 top_nodes: int = 9, refill_busy: int = 0,
                  options: Optional[RenderOptions] = None) -> RenderOptions:
     """crt_render_options from keywords; `options` (e.g. the autotuner's
     choice) overrides them all."""
@@ -266,7 +266,7 @@ class GB300Renderer:
                  mode: str = "megakernel", view_id: int = 0, wave_paths: int = 0,
                  flags: int = 0, wave_sets: int = 0, block_size: int = 0,
                  stack_depth: int = 0, node_format: Optional[str] = None,
-                 queue_chunk: int = 0, top_nodes: int = 0, refill_busy: int = 0,
+                 queue_chunk: int = 0, top_nodes: int = 9, refill_busy: int = 0,
                  options: Optional[RenderOptions] = None):
         L = load()
         self.scene = scene

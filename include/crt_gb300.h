@@ -312,7 +312,7 @@ typedef struct {
                                   ~4.7 GB of path state per set) */
     uint32_t flags;            /* CRT_FLAG_* */
     uint32_t wave_sets;        /* wavefront: waves in flight at once, each with its
-                                  own buffers and stream, 0..8 (0 = default 3) */
+                                  own buffers and stream, 0..8 (0 = default 4) */
     uint32_t stack_depth;      /* wavefront traversal kernels: stack entries per
                                   thread kept in shared memory, 4..32 (0 = 8);
                                   deeper entries go to local memory */
@@ -323,7 +323,8 @@ typedef struct {
     uint32_t top_nodes;        /* wavefront traversal kernels: the first top_nodes
                                   BVH nodes (breadth-first: the top levels) are
                                   copied to shared memory at kernel start, 0..128
-                                  (0 = none; 9 = two levels, 73 = three) */
+                                  (0 = none; 9 = two levels, the default of
+                                  crt_render_options_default; 73 = three) */
     uint32_t refill_busy;      /* with CRT_FLAG_LANE_REFILL: idle lanes of a warp
                                   take new rays together once at most this many
                                   lanes are still busy, 1..31 (0 = 31: as soon as

@@ -67,7 +67,7 @@ def test_f32_nodes_render_identically(cuda, mode):
 @pytest.mark.parametrize("shape", [dict(block_size=64), dict(block_size=256),
                                    dict(stack_depth=4), dict(stack_depth=32, block_size=256),
                                    dict(node_format="f32"), dict(wave_sets=1), dict(wave_sets=8),
-                                   dict(top_nodes=9), dict(top_nodes=73, node_format="f32"),
+                                   dict(top_nodes=0), dict(top_nodes=9), dict(top_nodes=73, node_format="f32"),
                                    dict(top_nodes=128, block_size=64, queue_chunk=128)])
 def test_launch_shape_does_not_change_results(cuda, shape):
     """Block size, shared stack depth, per-render node format and the
