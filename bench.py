@@ -615,15 +615,20 @@ def run_gb300(args):
         peak, peak_kind = measured_peaks()
         node_bytes = NODE_BYTES if wf.options.node_format != 1 else F32_NODE_BYTES
         roof = {}
-        for stage, rays, nodes, tris in (("extend", "extension_rays", "extension_nodes", "extension_tris"),
-                                         ("shadow", "shadow_rays", "shadow_nodes", "shadow_tris")):
+        # algorithmic bytes of the gathers: visits to the nodes staged in
+        # shared memory (top_nodes) are counted apart, not as L1/L2 gathers
+        for stage, rays, nodes, tris, top in (
+                ("extend", "extension_rays", "extension_nodes", "extension_tris", "extension_top_nodes"),
+                ("shadow", "shadow_rays", "shadow_nodes", "shadow_tris", "shadow_top_nodes")):
             launches = prof[f"{stage}_launches"]
-            alg = prof[nodes] * node_bytes + prof[tris] * TRI_BYTES
+            alg = (prof[nodes] - prof[top]) * node_bytes + prof[tris] * TRI_BYTES
             ms_l = prof[f"{stage}_ms"] / launches
             gbs = alg / launches / (ms_l * 1e-3) / 1e9
             roof[stage] = {"kernel": "wf_" + stage, "bytes_per_launch": alg / launches,
                            "ms_per_launch": ms_l, "gbs": gbs, "rays": prof[rays],
                            "nodes_per_ray": prof[nodes] / max(prof[rays], 1),
+                           "staged_nodes_per_ray": prof[top] / max(prof[rays], 1),
+                           "shared_memory_bytes_per_launch": prof[top] * node_bytes / launches,
                            "tris_per_ray": prof[tris] / max(prof[rays], 1)}
         main = roof["extend"] if dom != "shadow" else roof["shadow"]
         traffic = None
@@ -639,8 +644,10 @@ def run_gb300(args):
         # L2-resident (64 MiB) working set, combined with the traversal's own
         # L1 sector hit rate (ncu, profiles/wf_extend_cache.json):
         # 1 / (h1 / BW_L1 + (1 - h1) / BW_L2), weighted by the byte mix
-        nb = prof["extension_nodes" if main["kernel"] == "wf_extend" else "shadow_nodes"] * node_bytes
-        tb = prof["extension_tris" if main["kernel"] == "wf_extend" else "shadow_tris"] * TRI_BYTES
+        ext_k = main["kernel"] == "wf_extend"
+        nb = (prof["extension_nodes" if ext_k else "shadow_nodes"]
+              - prof["extension_top_nodes" if ext_k else "shadow_top_nodes"]) * node_bytes
+        tb = prof["extension_tris" if ext_k else "shadow_tris"] * TRI_BYTES
         g1 = gather_ceiling(torch, stream, (node_bytes, TRI_BYTES), working_set=96 << 10, l1=True)
         g2 = gather_ceiling(torch, stream, (node_bytes, TRI_BYTES), working_set=64 << 20, l1=True)
         mix = lambda g: (nb + tb) / (nb / g[node_bytes] + tb / g[TRI_BYTES])
@@ -666,13 +673,17 @@ def run_gb300(args):
                             "peak_kind": f"{peak_kind} HBM copy; achieved = ncu DRAM traffic / time"},
                     "limiter": "divergent dependent gathers: see profiles/wf_extend_large_textured_1080p.md "
                                "(issue-active, SIMT lanes, long-scoreboard stalls)",
-                    "algorithmic_bytes": f"nodes visited x {node_bytes} B + triangles tested x 48 B per ray"}
+                    "algorithmic_bytes": f"nodes visited outside the shared-memory top nodes x {node_bytes} B "
+                                         "+ triangles tested x 48 B per ray",
+                    "staged_nodes_per_ray": round(main["staged_nodes_per_ray"], 3)}
         l2_peak = hier
         step_bytes = None
         if main["kernel"] == "wf_extend":
             # per-step cross-check: all traversal bytes of a step / its time
-            per_ray_ext = (roof["extend"]["nodes_per_ray"] * node_bytes + roof["extend"]["tris_per_ray"] * TRI_BYTES)
-            per_ray_shd = (roof["shadow"]["nodes_per_ray"] * node_bytes + roof["shadow"]["tris_per_ray"] * TRI_BYTES)
+            per_ray_ext = ((roof["extend"]["nodes_per_ray"] - roof["extend"]["staged_nodes_per_ray"]) * node_bytes
+                           + roof["extend"]["tris_per_ray"] * TRI_BYTES)
+            per_ray_shd = ((roof["shadow"]["nodes_per_ray"] - roof["shadow"]["staged_nodes_per_ray"]) * node_bytes
+                           + roof["shadow"]["tris_per_ray"] * TRI_BYTES)
             step_bytes = ext * per_ray_ext + shd * per_ray_shd
             roofline["step_check"] = {"traversal_bytes_per_step": round(step_bytes),
                                       "gbs_over_whole_step": round(step_bytes / (ms_step * 1e-3) / 1e9, 1),
@@ -780,7 +791,8 @@ def run_gb300(args):
                                    "seconds_per_step")}
         detail["roofline_line"] = dict(roofline)
         roofline = {k: roofline[k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac",
-                                             "traffic", "l2_only", "hbm", "step_check") if k in roofline}
+                                             "traffic", "l2_only", "hbm", "step_check", "staged_nodes_per_ray")
+                    if k in roofline}
         roofline["hbm"] = {k: roofline["hbm"][k] for k in ("achieved", "peak", "frac")}
         if c4:
             c4 = {"speedup": c4["speedup"],

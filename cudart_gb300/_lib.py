@@ -77,7 +77,8 @@ class StageProfile(C.Structure):
                 ("extension_tris", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("shadow_nodes", C.c_uint64), ("shadow_tris", C.c_uint64),
                 ("extend_ms_by_bounce", C.c_double * 16), ("extend_rays_by_bounce", C.c_uint64 * 16),
-                ("shadow_ms_by_bounce", C.c_double * 16), ("shadow_rays_by_bounce", C.c_uint64 * 16)]
+                ("shadow_ms_by_bounce", C.c_double * 16), ("shadow_rays_by_bounce", C.c_uint64 * 16),
+                ("extension_top_nodes", C.c_uint64), ("shadow_top_nodes", C.c_uint64)]
 
 
 class RenderOptions(C.Structure):

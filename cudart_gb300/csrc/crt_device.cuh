@@ -160,8 +160,11 @@ struct Hit {
     float u, v;
 };
 
+// Counting traversals: node visits, triangle tests, and visits to the first
+// top_limit nodes (those a staging kernel holds in shared memory).
 struct TraversalStats {
     uint32_t nodes, tris;
+    uint32_t top = 0, top_limit = 0;
 };
 
 // Dynamic shared memory of the traversal kernels that stage the top of the
@@ -422,7 +425,10 @@ struct Traversal {
             st.push(make_uint2(grp.x, (hits << 8) | imask));
         }
         if (++visits > kVisitCeiling) { atomicOr(S.error, ERR_WATCHDOG); return true; }
-        if (COUNT) stats->nodes++;
+        if (COUNT) {
+            stats->nodes++;
+            if (node < stats->top_limit) stats->top++;
+        }
 
         uint32_t child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask;
         if (F32) test_children_f32(S, node, st.n_top, child_base, child_imask, tri_base_new, meta_lo, meta_hi, hitmask);

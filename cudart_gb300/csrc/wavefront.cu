@@ -64,7 +64,10 @@ enum Counter : uint32_t {
 };
 
 // Profiling totals: extension rays, nodes, triangles; shadow rays, nodes, triangles.
-enum ProfileCounter : uint32_t { P_EXT_RAYS, P_EXT_NODES, P_EXT_TRIS, P_SHD_RAYS, P_SHD_NODES, P_SHD_TRIS, P_COUNT };
+// Visits to the staged top nodes: P_EXT_TOP, P_SHD_TOP.
+enum ProfileCounter : uint32_t {
+    P_EXT_RAYS, P_EXT_NODES, P_EXT_TRIS, P_SHD_RAYS, P_SHD_NODES, P_SHD_TRIS, P_EXT_TOP, P_SHD_TOP, P_COUNT
+};
 
 // Pixels [p0, p1) x samples [s0, s1) of view `view`: path slot0 +
 // seg_slot(k, s) carries sample s0 + s of the k-th pixel of the range
@@ -882,6 +885,11 @@ CRT_D void add_profile(unsigned long long* p, uint32_t rays, uint32_t nodes, uin
     }
 }
 
+CRT_D void add_top(unsigned long long* p, uint32_t top) {
+    const uint32_t t = __reduce_add_sync(0xFFFFFFFFu, top);
+    if ((threadIdx.x & 31u) == 0 && t) atomicAdd(p, (unsigned long long)t);
+}
+
 // Counting re-runs (profiling only): the same traversals as wf_extend /
 // wf_shadow over the same queue entries, tallying node visits and triangle
 // tests instead of writing results.
@@ -896,7 +904,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_extend_count(WaveParams W) {
     const QueueView q = queue_view(W, cur, pre_sh);
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t rays = 0;
-    TraversalStats ts{0, 0};
+    TraversalStats ts{0, 0, 0, W.top_nodes};
     for (;;) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&W.counters[C_FETCH_CNT], 32u);
@@ -916,6 +924,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_extend_count(WaveParams W) {
         }
     }
     add_profile(W.prof + P_EXT_RAYS, rays, ts.nodes, ts.tris);
+    add_top(W.prof + P_EXT_TOP, ts.top);
 }
 
 template <bool F32>
@@ -926,7 +935,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shadow_count(WaveParams W) {
     const uint32_t n = W.counters[C_SHADOW];
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t rays = 0;
-    TraversalStats ts{0, 0};
+    TraversalStats ts{0, 0, 0, W.top_nodes};
     for (;;) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&W.counters[C_FETCH_CNT], 32u);
@@ -945,6 +954,7 @@ __global__ void __launch_bounds__(kWaveBlock) wf_shadow_count(WaveParams W) {
         }
     }
     add_profile(W.prof + P_SHD_RAYS, rays, ts.nodes, ts.tris);
+    add_top(W.prof + P_SHD_TOP, ts.top);
 }
 
 int persistent_grid(const void* kernel, int block, size_t smem) {
@@ -1637,6 +1647,8 @@ int wavefront_profile_pass(crt_render r, const std::vector<ViewWork>& work, crt_
     out->shadow_rays += c[P_SHD_RAYS];
     out->shadow_nodes += c[P_SHD_NODES];
     out->shadow_tris += c[P_SHD_TRIS];
+    out->extension_top_nodes += c[P_EXT_TOP];
+    out->shadow_top_nodes += c[P_SHD_TOP];
     return CRT_OK;
 }
 

@@ -378,7 +378,7 @@ class GB300Renderer:
         out = {f"{s}_ms": p.ms[i] for i, s in enumerate(p.STAGES)}
         out.update({f"{s}_launches": p.launches[i] for i, s in enumerate(p.STAGES)})
         for f in ("extension_rays", "extension_nodes", "extension_tris", "shadow_rays",
-                  "shadow_nodes", "shadow_tris"):
+                  "shadow_nodes", "shadow_tris", "extension_top_nodes", "shadow_top_nodes"):
             out[f] = getattr(p, f)
         for f in ("extend_ms_by_bounce", "extend_rays_by_bounce", "shadow_ms_by_bounce",
                   "shadow_rays_by_bounce"):

@@ -389,6 +389,8 @@ typedef struct {
     uint64_t extend_rays_by_bounce[16];
     double shadow_ms_by_bounce[16];
     uint64_t shadow_rays_by_bounce[16];
+    uint64_t extension_top_nodes, shadow_top_nodes;   /* visits (in *_nodes) to the nodes
+                                                         staged in shared memory (top_nodes) */
 } crt_stage_profile;
 
 /* Renders n_spp more samples per pixel (like crt_render_pass, same result)
