@@ -1325,6 +1325,10 @@ static int capture_set_graph(crt_render r, WaveSet& set) {
 // handle replays it with one launch per pass while the number of waves, the
 // sets and their wave graphs stay the same (the wave descriptors are data:
 // each pass uploads its own).
+// Passes of more waves (tiny waves or huge passes) keep the per-wave stream
+// launches: a graph of ~45 nodes per wave would take long to instantiate.
+constexpr size_t kMaxPassGraphWaves = 1024;
+
 static int build_pass_graph(crt_render r, size_t n_waves, uint32_t K) {
     WaveGraph* pg = new WaveGraph();
     r->pass_graph = pg;
@@ -1384,7 +1388,7 @@ int wavefront_pass(crt_render r, const std::vector<ViewWork>& work) {
         }
     for (WaveSet& s : r->sets)
         if ((st = capture_set_graph(r, s)) != CRT_OK) return st;
-    if (plan.waves.size() <= chunk) {
+    if (plan.waves.size() <= std::min<size_t>(chunk, kMaxPassGraphWaves)) {
         // one upload of wave descriptors covers the pass: queue it and the
         // whole pass as one graph on the handle's stream
         for (uint32_t k = 0; k < K; ++k) {

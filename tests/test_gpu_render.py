@@ -108,6 +108,21 @@ def test_window_sort_renders_identically(cuda, extra):
     assert np.array_equal(out[1], mk.accum())
 
 
+def test_passes_of_many_waves_render_identically(cuda):
+    """A pass of up to 1024 waves runs as one graph launch; longer passes
+    (here 1050 waves of 4 samples) keep per-wave launches: both schedules
+    add every pixel's samples in sample order."""
+    sc = scenes.cornell_box(width=128, height=128)
+    g = GB300Scene(sc)
+    out = []
+    for spp in (4096, 4200):
+        wf = GB300Renderer(g, sc.width, sc.height, spp, max_depth=5, mode="wavefront", wave_paths=1 << 16)
+        wf.render(spp)
+        mk = GB300Renderer(g, sc.width, sc.height, spp, max_depth=5, mode="megakernel")
+        mk.render(spp)
+        assert np.array_equal(wf.accum(), mk.accum()), spp
+
+
 def test_four_wide_bvh_renders_identically(cuda):
     sc = scenes.mixed_mid(width=128, height=72, subdiv=3)
     a = GB300Renderer(GB300Scene(sc), 128, 72, 8, max_depth=8, mode="wavefront")
