@@ -114,7 +114,6 @@ def test_passes_of_many_waves_render_identically(cuda):
     add every pixel's samples in sample order."""
     sc = scenes.cornell_box(width=128, height=128)
     g = GB300Scene(sc)
-    out = []
     for spp in (4096, 4200):
         wf = GB300Renderer(g, sc.width, sc.height, spp, max_depth=5, mode="wavefront", wave_paths=1 << 16)
         wf.render(spp)
